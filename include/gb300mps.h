@@ -1,0 +1,181 @@
+/*
+ * gb300mps.h - C ABI of the GB300 matrix-product-state circuit engine.
+ *
+ * The engine replaces the numerical layer of TNQVM's MPS visitors: the
+ * per-gate loop of ExatnMpsVisitor (tnqvm/visitors/exatn-mps/ExaTnMpsVisitor.cpp)
+ * and ITensorMPSVisitor (tnqvm/visitors/itensor/mps/ITensorMPSVisitor.cpp).
+ * A C++ TNQVMVisitor plugin (tnqvm/visitors/TNQVMVisitor.hpp:58-82) records
+ * gates through this ABI and reads results back; nothing in these signatures
+ * is a C++ or torch type.  Every entry point returns an MPS_* status; on a
+ * non-zero status mps_last_error() describes the failure (thread-local).
+ *
+ * Conventions
+ *  - complex numbers are interleaved (re, im) doubles;
+ *  - a 1-qubit matrix is 2x2 row-major (8 doubles);
+ *  - a 2-qubit matrix is 4x4 row-major (32 doubles) and its first qubit
+ *    argument is the most significant bit of the row/column index, as in
+ *    tnqvm/base/Gates.hpp:238-246 (CNOT) and ExatnUtils.cpp:116-130;
+ *  - amplitude index bit q is qubit q (ExaTnMpsVisitor.cpp:616-634);
+ *  - sampled bit strings list qubits in Measure order
+ *    (tnqvm/utils/GateMatrixAlgebra.hpp:129-137).
+ */
+#ifndef GB300MPS_H
+#define GB300MPS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define MPS_OK 0
+#define MPS_ERR_ARG 1         /* invalid argument (xacc::error in the reference) */
+#define MPS_ERR_OOM 2         /* device memory or admission budget exhausted */
+#define MPS_ERR_TIMEOUT 3     /* mps_wait / serve poll ran out of time */
+#define MPS_ERR_NUMERIC 4     /* NaN/Inf or a failed numerical invariant */
+#define MPS_ERR_CUDA 5        /* CUDA runtime error */
+#define MPS_ERR_STATE 6       /* call out of order (e.g. measuring before submit) */
+#define MPS_ERR_UNSUPPORTED 7 /* size beyond what this build supports */
+
+/* truncation semantics */
+#define MPS_TRUNC_EXATN 0   /* ExaTnMpsVisitor.cpp:2366-2536: absolute per-index cut, sqrt(S) both sides */
+#define MPS_TRUNC_ITENSOR 1 /* ITensor decomp.cc:307-463: relative discarded weight, canonical form */
+
+/* arithmetic */
+#define MPS_PREC_FP64 0 /* complex128 storage and arithmetic */
+#define MPS_PREC_FP32 1 /* complex64 storage and arithmetic, FP64 reductions */
+
+/* program flags */
+#define MPS_FLAG_RENORM 1   /* rescale the kept part to the pre-truncation norm */
+#define MPS_FLAG_PER_GATE 2 /* one kernel launch per gate (the plain visitor path) */
+
+/* largest bond dimension the single-CTA gate kernel handles */
+#define MPS_CHI_LIMIT 64
+/* largest qubit count for mps_amplitudes */
+#define MPS_AMP_QUBITS_MAX 26
+
+typedef struct mps_ctx mps_ctx;
+typedef struct mps_prog mps_prog;
+
+typedef struct mps_cfg {
+  int device;               /* CUDA device ordinal */
+  size_t hbm_budget_bytes;  /* admission budget for resident MPS state (0 = 150 GB) */
+} mps_cfg;
+
+const char* mps_last_error(void);
+const char* mps_version(void);
+
+/* Context: owns the stream, scratch and every program's device memory.
+ * Replaces exatn::initialize (ExaTnMpsVisitor.cpp:187-255). */
+int mps_ctx_create(const mps_cfg* cfg, mps_ctx** out);
+int mps_ctx_destroy(mps_ctx* ctx);
+int mps_ctx_info(mps_ctx* ctx, int* num_sms, size_t* bytes_resident);
+
+/* Program = one MPS register plus the gates recorded on it.
+ * Replaces ExatnMpsVisitor::initialize (ExaTnMpsVisitor.cpp:173-345) and
+ * ITensorMPSVisitor::initialize (ITensorMPSVisitor.cpp:105-157):
+ * |0...0> with every bond of dimension 1.  chi_max <= 0 means "no cap"
+ * (clamped to MPS_CHI_LIMIT); cutoff < 0 selects the visitor's default
+ * (DBL_MIN for exatn, 1e-6 for itensor). */
+int mps_program_begin(mps_ctx* ctx, int n_qubits, int chi_max, double cutoff,
+                      int trunc_mode, int precision, int flags, mps_prog** out);
+int mps_program_reset(mps_prog* p); /* back to |0...0>, keeps the allocation */
+int mps_program_destroy(mps_prog* p);
+
+/* Gate recording.  Replaces the per-gate visit()/applyGate of
+ * ExaTnMpsVisitor.cpp:1185-1292 (1 qubit) and :1387-1730 (2 qubits).
+ * mps_gate2 accepts any pair of distinct qubits; non-adjacent pairs are
+ * routed with SWAPs as NearestNeighborTransform.hpp:43-135 does.
+ * mps_gate_named takes an XACC gate name (Gates.hpp:41-67 list, plus "CX",
+ * "U3", "S", "Sdg", "RZZ") and its parameters. */
+int mps_gate1(mps_prog* p, int qubit, const double m[8]);
+int mps_gate2(mps_prog* p, int q0, int q1, const double m[32]);
+int mps_gate_named(mps_prog* p, const char* name, const int* qubits, int n_qubits,
+                   const double* params, int n_params);
+int mps_measure(mps_prog* p, int qubit); /* ExaTnMpsVisitor.cpp:991-994 */
+/* Bulk recording: gate ids follow tnqvm::CommonGates (Gates.hpp:41-67),
+ * extended with MPS_G_RZZ; qubits holds 2 ints per gate (second ignored for
+ * 1-qubit gates), params 3 doubles per gate (unused ones ignored). */
+enum {
+  MPS_G_I = 0, MPS_G_H, MPS_G_CNOT, MPS_G_RX, MPS_G_RY, MPS_G_RZ, MPS_G_SWAP, MPS_G_U, MPS_G_X, MPS_G_Y,
+  MPS_G_Z, MPS_G_MEASURE, MPS_G_CZ, MPS_G_CPHASE, MPS_G_S, MPS_G_SDG, MPS_G_T, MPS_G_TDG, MPS_G_CY,
+  MPS_G_CH, MPS_G_CRZ, MPS_G_ISWAP, MPS_G_FSIM, MPS_G_RZZ, MPS_G_COUNT
+};
+int mps_gates(mps_prog* p, int n_gates, const int32_t* ids, const int32_t* qubits, const double* params);
+
+/* Execution.  mps_submit compiles the gates recorded since the previous
+ * submit (routing, 1-qubit fusion, gauge moves) and enqueues them; the MPS
+ * stays resident on the device across submits. */
+int mps_submit(mps_prog* p);
+int mps_wait(mps_prog* p, int timeout_ms);
+/* One persistent launch over many programs (circuits of any size/bond cap). */
+int mps_batch_submit(mps_ctx* ctx, mps_prog* const* progs, int n_progs);
+
+/* Results.  Replace finalize (ExaTnMpsVisitor.cpp:576-681), the state-vector
+ * contraction (:591-597), exp-val-z (:616-644) and ITensor's transfer-matrix
+ * expectation (ITensorMPSVisitor.cpp:173-250,440-464). */
+int mps_norm(mps_prog* p, double* out);                    /* <psi|psi> */
+int mps_amplitudes(mps_prog* p, double* out);              /* 2 * 2^n doubles */
+int mps_amplitude(mps_prog* p, const int* bits, double out[2]); /* one bit string */
+/* paulis: n_terms strings of n_qubits characters from "IXYZ", character i
+ * acting on qubit i, concatenated.  out: 2*n_terms doubles (<P_t> re,im,
+ * unnormalised), then, if coeffs != NULL, sum_t coeffs[t]*Re<P_t>. */
+int mps_expect_pauli(mps_prog* p, const char* paulis, int n_terms,
+                     const double* coeffs, double* out);
+/* Observable attached to a program, evaluated for many programs at once by
+ * mps_batch_expect (out[i] = sum_t c_t Re<P_t>/<psi|psi> for program i). */
+int mps_set_observable(mps_prog* p, const char* paulis, int n_terms, const double* coeffs);
+int mps_batch_expect(mps_ctx* ctx, mps_prog* const* progs, int n_progs, double* out);
+/* Shot sampling from the MPS with a counter-based RNG; bits is
+ * shots * n_measured bytes (0/1); without Measure records every qubit is
+ * measured in order.  Replaces getMeasureSample (ExaTnMpsVisitor.cpp:2211-2364)
+ * and GenerateSamples (GateMatrixAlgebra.hpp:125-156). */
+int mps_sample(mps_prog* p, int shots, uint64_t seed, uint8_t* bits);
+int mps_n_measured(mps_prog* p, int* out);
+/* product over 2-qubit gates of (1 - discarded weight fraction) */
+int mps_truncation_fidelity(mps_prog* p, double* out);
+int mps_bond_dims(mps_prog* p, int* out); /* n_qubits-1 ints */
+int mps_stats(mps_prog* p, double out[4]); /* fidelity, max discarded, #2q gates, #ops */
+
+/* Captured batch (CUDA graph).  mps_graph_create consumes the gates recorded
+ * on each program and captures: reset to |0...0>, one persistent launch over
+ * all programs, the attached observables, and the copy of the energies to
+ * host.  mps_graph_launch replays it (energies[i] as in mps_batch_expect);
+ * mps_graph_update re-reads newly recorded gates of the same structure
+ * (e.g. new VQE parameters) into the captured op table. */
+typedef struct mps_graph mps_graph;
+int mps_graph_create(mps_ctx* ctx, mps_prog* const* progs, int n_progs, mps_graph** out);
+int mps_graph_launch(mps_graph* g, double* energies);
+int mps_graph_launch_async(mps_graph* g);
+int mps_graph_sync(mps_graph* g, double* energies);
+int mps_graph_update(mps_graph* g);
+int mps_graph_stream(mps_graph* g, void** cuda_stream);
+/* Device time of the last replay from CUDA events captured in the graph:
+ * out[0] reset + fused op kernel, out[1] observables (+ copy), in ms; out[2]
+ * algorithmic GEMM-class flops of the op kernel (theta merge + gate + Gram +
+ * split, eigensolver excluded), out[3] eigensolver rotation flops. */
+int mps_graph_timing(mps_graph* g, double out[4]);
+int mps_graph_destroy(mps_graph* g);
+
+/* Continuous-batching request loop (serving).  Requests are programs that
+ * have recorded gates and optionally an observable and a shot count; the
+ * loop admits them by projected HBM footprint, runs them in overlapping
+ * persistent launches and completes them out of order. */
+int mps_serve_start(mps_ctx* ctx, int max_inflight);
+int mps_serve_submit(mps_ctx* ctx, mps_prog* p, int shots, uint64_t seed, uint64_t* ticket);
+/* Polls a ticket: returns MPS_OK when done (result written), MPS_ERR_TIMEOUT
+ * if not finished within timeout_ms. energy may be NULL; bits (shots*n_meas)
+ * may be NULL. */
+int mps_serve_poll(mps_ctx* ctx, uint64_t ticket, int timeout_ms, double* energy,
+                   uint8_t* bits, double* latency_ms);
+int mps_serve_stop(mps_ctx* ctx);
+
+/* Footprint used by admission: sum over sites of chi_l * 2 * chi_r * bytes. */
+size_t mps_footprint_bytes(int n_qubits, int chi_max, int precision);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GB300MPS_H */

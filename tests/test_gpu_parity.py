@@ -1,0 +1,348 @@
+"""GPU parity: the sm_103a engine, called through the C ABI, against the CPU
+oracle on the same seeded inputs.  Tolerances are stated per test: 1e-10 for
+complex128 runs against the complex128 oracle, 2e-5 for complex64 runs."""
+import numpy as np
+import pytest
+
+from oracle import dense, routing
+from oracle import mps as omps
+from tnqvm_gb300 import circuits
+from tnqvm_gb300 import mps as M
+from tnqvm_gb300.visitor import AcceleratorBuffer, GpuMpsVisitor
+
+pytestmark = pytest.mark.gpu
+
+PI = np.pi
+TOL64 = 1e-10
+TOL32 = 2e-5
+
+
+def run(ctx, n, circ, chi=0, cutoff=-1.0, mode=M.TRUNC_EXATN, prec=M.PREC_FP64, flags=0):
+    p = M.Program(ctx, n, chi, cutoff, mode, prec, flags)
+    p.run(circ)
+    p.submit()
+    p.wait()
+    return p
+
+
+def zstr(n, qs):
+    s = ["I"] * n
+    for q in qs:
+        s[q] = "Z"
+    return "".join(s)
+
+
+# ----------------------------------------------------------------- exact runs
+@pytest.mark.parametrize("mode", [M.TRUNC_EXATN, M.TRUNC_ITENSOR])
+@pytest.mark.parametrize("flags", [0, M.FLAG_PER_GATE])
+def test_brickwall12_exact_fp64(ctx, mode, flags):
+    """12 qubits, depth 20, U3 + CNOT brick wall, chi 64 (exact), cutoff 1e-14:
+    every amplitude and every <Z_i> against the dense oracle."""
+    n = 12
+    circ = circuits.brickwall(n, 20, seed=11)
+    psi = dense.run(n, circ)
+    with run(ctx, n, circ, 64, 1e-14, mode, M.PREC_FP64, flags) as p:
+        amp = p.amplitudes()
+        assert np.max(np.abs(amp - psi)) < TOL64
+        zs = p.expect_pauli([zstr(n, [q]) for q in range(n)])
+        for q in range(n):
+            assert abs(zs[q].real - dense.expect_z_parity(psi, [q])) < TOL64
+        assert abs(p.norm() - 1.0) < TOL64
+
+
+@pytest.mark.parametrize("mode", [M.TRUNC_EXATN, M.TRUNC_ITENSOR])
+def test_brickwall12_exact_fp32(ctx, mode):
+    n = 12
+    circ = circuits.brickwall(n, 20, seed=11)
+    psi = dense.run(n, circ)
+    with run(ctx, n, circ, 64, 1e-14, mode, M.PREC_FP32) as p:
+        amp = p.amplitudes()
+        assert np.max(np.abs(amp - psi)) < TOL32
+        zs = p.expect_pauli([zstr(n, [q]) for q in range(n)])
+        for q in range(n):
+            assert abs(zs[q].real - dense.expect_z_parity(psi, [q])) < TOL32
+
+
+# ------------------------------------------------------------- truncated runs
+@pytest.mark.parametrize("mode,omode", [(M.TRUNC_ITENSOR, "itensor"), (M.TRUNC_EXATN, "exatn")])
+@pytest.mark.parametrize("chi", [4, 8, 16])
+def test_truncated_fp64_vs_oracle(ctx, mode, omode, chi):
+    n = 10
+    circ = circuits.brickwall(n, 8, seed=5)
+    ref = omps.run(n, routing.route(circ), mode=omode, chi_max=chi, cutoff=1e-12)
+    paulis = ["XYZIZXYIZX", "ZZIIIIIIII", "IIIIZZIIII", "YIIIIIIIIY", "IIIIIIIIII"]
+    with run(ctx, n, circ, chi, 1e-12, mode, M.PREC_FP64) as p:
+        assert p.bond_dims() == ref.bond_dims()
+        vals = p.expect_pauli(paulis)
+        for s, v in zip(paulis, vals):
+            assert abs(v - ref.expect_pauli(s)) < 1e-9, s
+        assert abs(p.truncation_fidelity() - ref.fidelity) < 1e-9
+
+
+def test_hea_truncated_fp32_vs_fp64_oracle(ctx):
+    """The complex64 engine with canonical truncation against the complex128
+    oracle at the same cap: |dE| <= 1e-6 on a 50-term Hamiltonian."""
+    rng = np.random.default_rng(9)
+    n = 16
+    circ = circuits.hea(n, 9, seed=4)
+    paulis, coeffs = circuits.random_paulis(n, 50, rng)
+    ref = omps.run(n, routing.route(circ), mode="itensor", chi_max=32, cutoff=0.0)
+    e_ref = sum(c * ref.expect_pauli(s).real for s, c in zip(paulis, coeffs)) / ref.norm2()
+    with run(ctx, n, circ, 32, 0.0, M.TRUNC_ITENSOR, M.PREC_FP32) as p:
+        p.set_observable(paulis, coeffs)
+        e = ctx.batch_expect([p])[0]
+        assert abs(e - e_ref) < 1e-6
+
+
+# ------------------------------------------------- reference golden values
+def visitor_run(ctx, n, circ, shots=0, **opts):
+    v = GpuMpsVisitor(ctx)
+    v.setOptions(opts)
+    buf = AcceleratorBuffer(n)
+    v.initialize(buf, shots)
+    v.run(circ)
+    v.finalize()
+    return buf, v
+
+
+def linspace(a, b, n):
+    return [a + (b - a) * i / (n - 1) for i in range(n)]
+
+
+def test_rotation_goldens(ctx):
+    # ITensorMPSVisitorTester.cpp:321-391 (1e-6)
+    for t in linspace(-PI, PI, 20):
+        want = 1 - 2 * np.sin(t / 2) ** 2
+        for circ, n, mq in (([("Rx", (0,), (t,)), ("Measure", (0,), ())], 1, 0),
+                            ([("U", (0,), (t, -PI / 2, PI / 2)), ("Measure", (0,), ())], 1, 0),
+                            ([("X", (0,), ()), ("H", (1,), ()), ("CPhase", (0, 1), (t,)), ("H", (1,), ()),
+                              ("Measure", (1,), ())], 2, 1)):
+            buf, _ = visitor_run(ctx, n, circ, shots=0)
+            assert abs(buf.getExpectationValueZ() - want) < 1e-6
+
+
+def test_deuteron_table_gpu(ctx):
+    from tests.test_oracle_golden import DEUTERON_X0X1
+    for i, t in enumerate(linspace(-PI, PI, 20)):
+        circ = [("X", (0,), ()), ("Ry", (1,), (t,)), ("CNOT", (1, 0), ()), ("H", (0,), ()), ("H", (1,), ()),
+                ("Measure", (0,), ()), ("Measure", (1,), ())]
+        buf, _ = visitor_run(ctx, 2, circ, shots=0)
+        assert abs(buf.getExpectationValueZ() - DEUTERON_X0X1[i]) < 1e-5
+
+
+def test_ghz_amplitude_bitstring(ctx):
+    # ITensorMPSVisitorTester.cpp:522-551 through the bitstring option (ExaTnMpsVisitor.cpp:776-822)
+    circ = [("H", (0,), ()), ("Z", (0,), ()), ("CNOT", (0, 1), ()), ("CNOT", (1, 2), ())]
+    buf, _ = visitor_run(ctx, 3, circ, bitstring=[1, 1, 1])
+    assert abs(buf["amplitude-real"] + 1 / np.sqrt(2)) < 1e-6 and abs(buf["amplitude-imag"]) < 1e-6
+    buf, _ = visitor_run(ctx, 3, circ, bitstring=[-1, 1, 1])
+    assert np.allclose(buf["amplitude-real-vec"], [0.0, -1.0], atol=1e-9)
+
+
+def test_sampled_gate_goldens(ctx):
+    # MpsGateTester.cpp: 10k shots, 0.05 / 0.01 tolerances
+    for q in range(4):
+        circ = [("H", (q,), ())] + [("Measure", (i,), ()) for i in range(4)]
+        buf, _ = visitor_run(ctx, 4, circ, shots=10000, seed=q + 1)
+        one = ["0"] * 4
+        one[q] = "1"
+        assert abs(buf.computeMeasurementProbability("0000") - 0.5) < 0.05
+        assert abs(buf.computeMeasurementProbability("".join(one)) - 0.5) < 0.05
+    circ = [("X", (0,), ()), ("CNOT", (0, 3), ())] + [("Measure", (i,), ()) for i in range(4)]
+    buf, _ = visitor_run(ctx, 4, circ, shots=10000, seed=5)
+    assert abs(buf.computeMeasurementProbability("1001") - 1.0) < 0.01
+    circ = [("X", (0,), ()), ("iSwap", (0, 1), ())] + [("Measure", (i,), ()) for i in range(3)]
+    buf, _ = visitor_run(ctx, 3, circ, shots=100, seed=6)
+    assert abs(buf.computeMeasurementProbability("010") - 1.0) < 0.01
+    for a in linspace(-PI, PI, 10):
+        circ = [("X", (0,), ()), ("fSim", (0, 1), (a, 0.0)), ("Measure", (0,), ()), ("Measure", (1,), ())]
+        buf, _ = visitor_run(ctx, 2, circ, shots=1000, seed=7)
+        assert abs(buf.computeMeasurementProbability("01") - np.sin(a) ** 2) < 0.1
+        assert abs(buf.computeMeasurementProbability("10") - (1 - np.sin(a) ** 2)) < 0.1
+
+
+def test_grover_gpu(ctx):
+    from tests.test_oracle_golden import grover_circuit
+    circ = grover_circuit() + [("Measure", (2,), ()), ("Measure", (1,), ()), ("Measure", (0,), ())]
+    buf, _ = visitor_run(ctx, 3, circ, shots=10000, seed=3)
+    assert buf.computeMeasurementProbability("110") > 0.5
+
+
+def test_ghz35_samples(ctx):
+    # MpsMeasurementTester.cpp:7-35: 35-qubit GHZ, only 0...0 and 1...1
+    n = 35
+    circ = [("H", (0,), ())] + [("CNOT", (i, i + 1), ()) for i in range(n - 1)]
+    circ += [("Measure", (i,), ()) for i in range(n)]
+    buf, _ = visitor_run(ctx, n, circ, shots=200, seed=9)
+    counts = buf.getMeasurementCounts()
+    assert set(counts) <= {"0" * n, "1" * n}
+    assert abs(counts.get("0" * n, 0) / 200 - 0.5) < 0.15
+
+
+def test_seed_determinism(ctx):
+    # MpsMeasurementTester.cpp:37-66: the same seed gives identical samples
+    circ = circuits.brickwall(6, 4, seed=2)
+    with run(ctx, 6, circ) as p:
+        a = p.sample(500, seed=123)
+        for _ in range(5):
+            assert np.array_equal(p.sample(500, seed=123), a)
+        assert not np.array_equal(p.sample(500, seed=124), a)
+
+
+def test_sampling_chi_square(ctx):
+    """Histogram of 40000 shots against the exact distribution (chi-square)."""
+    from scipy.stats import chisquare
+    n = 7
+    circ = circuits.brickwall(n, 5, seed=21)
+    psi = dense.run(n, circ)
+    probs = dense.probabilities(psi, list(range(n)))
+    with run(ctx, n, circ, prec=M.PREC_FP32) as p:
+        bits = p.sample(40000, seed=77)
+    keys = (bits.astype(np.int64) << np.arange(n)).sum(axis=1)
+    obs = np.bincount(keys, minlength=1 << n)
+    mask = probs * 40000 > 5
+    exp = probs[mask] * 40000
+    exp = exp * obs[mask].sum() / exp.sum()
+    stat, pval = chisquare(obs[mask], exp)
+    assert pval > 1e-4, (stat, pval)
+
+
+def test_rcs_norm(ctx):
+    # NumericalTesterCheckNorm.cpp:15-62: norm = 1 +- 1e-6 for a 10-qubit, 15-layer RCS
+    circ = circuits.brickwall(10, 15, seed=8)
+    for cut in (-1.0, 1e-8):
+        with run(ctx, 10, circ, 0, cut) as p:
+            assert abs(p.norm() - 1.0) < 1e-6
+
+
+# ---------------------------------------------------------- batch and serve
+def test_batch_equals_individual(ctx):
+    insts = circuits.vqe_batch(instances=24, seed=3, qmin=4, qmax=14, lmin=2, lmax=7, terms=10)
+    progs, alone = [], []
+    for it in insts:
+        p = M.Program(ctx, it["n"], 16, 0.0, M.TRUNC_ITENSOR, M.PREC_FP32)
+        p.run(it["circuit"])
+        p.set_observable(it["paulis"], it["coeffs"])
+        progs.append(p)
+    ctx.batch_submit(progs)
+    e_batch = ctx.batch_expect(progs)
+    for it in insts:
+        p = M.Program(ctx, it["n"], 16, 0.0, M.TRUNC_ITENSOR, M.PREC_FP32)
+        p.run(it["circuit"])
+        p.submit()
+        p.set_observable(it["paulis"], it["coeffs"])
+        alone.append(ctx.batch_expect([p])[0])
+        p.close()
+    assert np.max(np.abs(e_batch - np.array(alone))) < 1e-12
+    for it, e in zip(insts, e_batch):
+        ref = omps.run(it["n"], it["circuit"], mode="itensor", chi_max=16, cutoff=0.0)
+        er = sum(c * ref.expect_pauli(s).real for s, c in zip(it["paulis"], it["coeffs"])) / ref.norm2()
+        assert abs(e - er) < 1e-5
+    for p in progs:
+        p.close()
+
+
+def test_serve_same_alone_and_in_mix(ctx):
+    insts = circuits.vqe_batch(instances=40, seed=8, qmin=4, qmax=16, lmin=2, lmax=8, terms=5)
+
+    def make(it):
+        p = M.Program(ctx, it["n"], 16, 0.0, M.TRUNC_ITENSOR, M.PREC_FP32)
+        p.run(it["circuit"])
+        p.set_observable(it["paulis"], it["coeffs"])
+        return p
+
+    alone = []
+    ctx.serve_start(64)
+    try:
+        for it in insts[:8]:
+            p = make(it)
+            t = ctx.serve_submit(p, 64, 5)
+            e, bits, lat = ctx.serve_poll(t, p, 64)
+            alone.append((e, bits.copy()))
+            p.close()
+        progs = [make(it) for it in insts]
+        tickets = [ctx.serve_submit(p, 64 if i < 8 else 0, 5) for i, p in enumerate(progs)]
+        for i, (t, p) in enumerate(zip(tickets, progs)):
+            e, bits, lat = ctx.serve_poll(t, p, 64 if i < 8 else 0)
+            assert lat >= 0.0
+            if i < 8:
+                assert abs(e - alone[i][0]) < 1e-9
+                assert np.array_equal(bits, alone[i][1])
+        for p in progs:
+            p.close()
+    finally:
+        ctx.serve_stop()
+
+
+# ------------------------------------------------------- errors and edges
+def test_errors(ctx):
+    with pytest.raises(M.MpsError) as e:
+        M.Program(ctx, 10, 65)
+    assert e.value.code == M.ERR_UNSUPPORTED
+    with M.Program(ctx, 3) as p:
+        with pytest.raises(M.MpsError) as e:
+            p.gate("CNOT", [0, 3])
+        assert e.value.code == M.ERR_ARG
+        with pytest.raises(M.MpsError):
+            p.gate("NotAGate", [0])
+        with pytest.raises(M.MpsError):
+            p.gate("Rx", [0])               # missing parameter
+        with pytest.raises(M.MpsError):
+            p.gate("CNOT", [1, 1])
+        with pytest.raises(M.MpsError):
+            p.expect_pauli(["XQZ"])
+
+
+def test_edges(ctx):
+    with M.Program(ctx, 1) as p:          # one qubit, no bonds
+        p.gate("H", [0])
+        p.gate("Rz", [0], [0.3])
+        amp = p.amplitudes()
+        assert np.allclose(amp, dense.run(1, [("H", (0,), ()), ("Rz", (0,), (0.3,))]), atol=1e-12)
+    with M.Program(ctx, 5) as p:          # empty circuit
+        assert abs(p.norm() - 1.0) < 1e-14
+        assert np.allclose(p.sample(10, 1), 0)
+    circ = [("H", (3,), ()), ("Swap", (3, 0), ()), ("CNOT", (4, 1), ()), ("iSwap", (2, 0), ()),
+            ("fSim", (1, 4), (0.3, 0.2)), ("CRZ", (0, 4), (0.7,)), ("CH", (2, 3), ()), ("CY", (3, 1), ()),
+            ("T", (0,), ()), ("Tdg", (1,), ()), ("S", (2,), ()), ("Sdg", (3,), ()), ("I", (4,), ())]
+    psi = dense.run(5, circ)
+    for mode in (M.TRUNC_EXATN, M.TRUNC_ITENSOR):
+        for prec, tol in ((M.PREC_FP64, TOL64), (M.PREC_FP32, TOL32)):
+            with run(ctx, 5, circ, 0, -1.0, mode, prec) as p:
+                assert np.max(np.abs(p.amplitudes() - psi)) < tol
+                bits = [int(b) for b in "10110"]
+                k = sum(b << i for i, b in enumerate(bits))
+                assert abs(p.amplitude(bits) - psi[k]) < tol
+
+
+def test_resident_state_across_submits(ctx):
+    """Gates recorded after a submit continue on the resident MPS."""
+    n = 8
+    c1 = circuits.brickwall(n, 3, seed=1)
+    c2 = circuits.brickwall(n, 3, seed=2)
+    with M.Program(ctx, n, 0, -1.0, M.TRUNC_ITENSOR) as p:
+        p.run(c1)
+        p.submit()
+        p.run(c2)
+        p.submit()
+        p.wait()
+        assert np.max(np.abs(p.amplitudes() - dense.run(n, c1 + c2))) < TOL64
+        p.reset()
+        p.run(c2)
+        assert np.max(np.abs(p.amplitudes() - dense.run(n, c2))) < TOL64
+
+
+def test_vqe_mode_observed_circuits(ctx):
+    """getExpectationValueZ with basis-change circuits equals <P> from the oracle."""
+    n = 4
+    circ = circuits.hea(n, 3, seed=6)
+    psi = dense.run(n, circ)
+    v = GpuMpsVisitor(ctx)
+    v.setOptions({"truncation-mode": "itensor"})
+    buf = AcceleratorBuffer(n)
+    v.initialize(buf, 0)
+    v.run(circ)
+    obs = [("H", (0,), ()), ("Rx", (2,), (PI / 2,)), ("Measure", (0,), ()), ("Measure", (1,), ()),
+           ("Measure", (2,), ())]
+    e = v.getExpectationValueZ(obs)
+    assert abs(e - dense.expect_pauli(psi, n, "XZYI").real) < TOL64

@@ -1,0 +1,158 @@
+// Internal host structures of the GB300 MPS engine.
+#pragma once
+#include <atomic>
+#include <condition_variable>
+#include <deque>
+#include <map>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "gates.hpp"
+#include "mps_common.cuh"
+
+namespace gbmps {
+
+// kernels (k_ops.cu, k_measure.cu)
+size_t op_scratch_bytes(int prec);
+size_t op_smem_bytes(int prec);
+cudaError_t launch_ops(int prec, const ProgDesc* d_progs, int n_progs, int grid, int* d_queue, char* scratch,
+                       cudaStream_t st);
+cudaError_t configure_ops();
+cudaError_t configure_expect();
+cudaError_t launch_reset(int prec, const ProgDesc* d_progs, int n_progs, cudaStream_t st);
+size_t expect_smem_bytes(int prec);
+size_t expect_scratch_bytes(int prec);
+cudaError_t launch_expect(int prec, const ExpTask* d_tasks, int n_tasks, char* scratch, double* d_out,
+                          cudaStream_t st);
+cudaError_t launch_right_env(int prec, const EnvTask& tk, char* scratch, cudaStream_t st);
+cudaError_t launch_sample(int prec, const SampleTask& tk, cudaStream_t st);
+cudaError_t launch_amp_step(int prec, const void* A, int dl, int dr, int k, const void* vin, void* vout,
+                            cudaStream_t st);
+cudaError_t launch_to_f64(int prec, const void* v, double* out, int64_t n, cudaStream_t st);
+cudaError_t launch_amp_one(int prec, const void* sites, const int64_t* site_off, const int* bond, const int* bits,
+                           int n, double* out, cudaStream_t st);
+
+// A lane is a stream with its own scratch and staging buffers, so work on
+// different lanes can overlap on the device.
+struct Lane {
+  cudaStream_t stream = nullptr;
+  char* op_scratch[2] = {nullptr, nullptr};
+  int op_scratch_ctas[2] = {0, 0};
+  char* exp_scratch[2] = {nullptr, nullptr};
+  int exp_scratch_ctas[2] = {0, 0};
+  DevOp* d_ops = nullptr;
+  size_t d_ops_cap = 0;
+  ProgDesc* d_desc = nullptr;
+  size_t d_desc_cap = 0;
+  ExpTask* d_exp_tasks = nullptr;
+  size_t d_exp_tasks_cap = 0;
+  double* d_exp_out = nullptr;
+  size_t d_exp_out_cap = 0;
+  char* d_work = nullptr;  // sampler environments, bits, offsets
+  size_t d_work_cap = 0;
+  int* d_queue = nullptr;
+  // pinned host staging
+  DevOp* h_ops = nullptr;
+  size_t h_ops_cap = 0;
+  ProgDesc* h_desc = nullptr;
+  size_t h_desc_cap = 0;
+};
+
+struct mps_prog_impl;
+
+struct ServeReq {
+  uint64_t ticket;
+  struct ::mps_prog* prog;
+  int shots;
+  uint64_t seed;
+  double t_submit;
+  double t_done;
+  int status;
+  double energy;
+  std::vector<uint8_t> bits;
+  bool done;
+};
+
+struct ServeBatch {
+  int lane;
+  std::vector<ServeReq*> reqs;
+  cudaEvent_t ev;
+  std::vector<ExpTask> tasks;
+  double* h_exp = nullptr;     // pinned, 2 doubles per task
+  size_t h_exp_cap = 0;
+  std::vector<std::pair<ServeReq*, uint8_t*>> bit_dst;
+  uint8_t* h_bits = nullptr;   // pinned
+  size_t h_bits_cap = 0;
+  size_t footprint = 0;
+};
+
+struct ServeState {
+  std::thread worker;
+  std::mutex mu;
+  std::condition_variable cv_work, cv_done;
+  std::deque<ServeReq*> queue;
+  std::map<uint64_t, ServeReq*> all;
+  std::vector<Lane> lanes;
+  std::vector<ServeBatch> batches;  // one slot per lane
+  std::vector<char> lane_busy;
+  uint64_t next_ticket = 1;
+  bool stop = false;
+  bool running = false;
+  int max_inflight = 256;
+  size_t inflight_bytes = 0;
+  int inflight_reqs = 0;
+};
+
+}  // namespace gbmps
+
+struct mps_ctx {
+  int device = 0;
+  int num_sms = 0;
+  size_t budget = 0;
+  size_t resident = 0;
+  std::mutex mu;
+  gbmps::Lane lane0;
+  gbmps::ServeState* serve = nullptr;
+};
+
+struct mps_prog {
+  mps_ctx* ctx = nullptr;
+  int n = 0, chi_cap = 0, mode = 0, prec = 0, flags = 0;
+  double cutoff = 0.0;
+  std::vector<gbmps::GateRec> pending;
+  std::vector<int> measured;
+  std::vector<int> cap_bond;
+  std::vector<int64_t> off;
+  size_t bytes = 0;
+  void* d_sites = nullptr;
+  char* d_meta = nullptr;
+  double* d_stats = nullptr;
+  int64_t* d_off = nullptr;
+  int* d_bond = nullptr;
+  int* d_err = nullptr;
+  cudaEvent_t ev = nullptr;
+  bool submitted = false;
+  int center = 0;
+  uint8_t* d_obs = nullptr;
+  std::vector<double> obs_coef;
+  int n_terms = 0;
+};
+
+namespace gbmps {
+extern thread_local std::string g_err;
+int fail(int code, const std::string& msg);
+size_t footprint(int n, int chi, int prec);
+void compile_program(::mps_prog* p, std::vector<DevOp>& ops);
+int lane_init(Lane& L);
+void lane_free(Lane& L);
+int launch_programs(mps_ctx* c, Lane& L, ::mps_prog* const* progs, int n, bool per_gate);
+int enqueue_expect(Lane& L, const std::vector<ExpTask>& tasks, int prec, double* h_out);
+int enqueue_sample(Lane& L, ::mps_prog* p, int shots, uint64_t seed, uint8_t* h_all_bits);
+int prog_check_err(::mps_prog* p);
+int parse_paulis(int n, const char* paulis, int n_terms, std::vector<uint8_t>& codes);
+void select_measured(const ::mps_prog* p, const uint8_t* all, int shots, uint8_t* bits);
+void observable_tasks(::mps_prog* p, std::vector<ExpTask>& tasks);
+double observable_value(const ::mps_prog* p, const double* r);
+}  // namespace gbmps

@@ -1,0 +1,260 @@
+// Captured batches: one CUDA graph per batch of programs, replayed for every
+// parameter update (the batched-VQE loop).  Body: reset every program to
+// |0...0> on the device, one persistent launch of the fused op kernel over
+// all programs, the expectation sweep of every attached observable, and the
+// copy of the raw expectation values to pinned host memory.
+#include <algorithm>
+#include <cstring>
+
+#include "../../include/gb300mps.h"
+#include "engine_internal.hpp"
+
+struct mps_graph {
+  mps_ctx* c = nullptr;
+  gbmps::Lane L;
+  std::vector<mps_prog*> progs;
+  int prec = 0;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  std::vector<gbmps::DevOp> flat;
+  std::vector<size_t> first, count;
+  std::vector<gbmps::ExpTask> tasks;
+  std::vector<size_t> task_first;
+  double* h_out = nullptr;
+  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+};
+
+namespace gbmps {
+
+static int build_ops(mps_graph* g, std::vector<DevOp>& flat, std::vector<size_t>& first, std::vector<size_t>& count) {
+  flat.clear();
+  first.assign(g->progs.size(), 0);
+  count.assign(g->progs.size(), 0);
+  std::vector<DevOp> ops;
+  for (size_t i = 0; i < g->progs.size(); ++i) {
+    mps_prog* p = g->progs[i];
+    p->center = 0;  // every replay starts from |0...0>
+    compile_program(p, ops);
+    first[i] = flat.size();
+    count[i] = ops.size();
+    flat.insert(flat.end(), ops.begin(), ops.end());
+  }
+  return MPS_OK;
+}
+
+}  // namespace gbmps
+
+using namespace gbmps;
+
+#define GCK(call)                                                             \
+  do {                                                                        \
+    cudaError_t e_ = (call);                                                  \
+    if (e_ != cudaSuccess) return fail(MPS_ERR_CUDA, cudaGetErrorString(e_)); \
+  } while (0)
+
+extern "C" {
+
+int mps_graph_destroy(mps_graph* g) {
+  if (!g) return MPS_OK;
+  cudaSetDevice(g->c->device);
+  if (g->L.stream) cudaStreamSynchronize(g->L.stream);
+  if (g->exec) cudaGraphExecDestroy(g->exec);
+  if (g->graph) cudaGraphDestroy(g->graph);
+  if (g->h_out) cudaFreeHost(g->h_out);
+  for (int i = 0; i < 3; ++i)
+    if (g->ev[i]) cudaEventDestroy(g->ev[i]);
+  lane_free(g->L);
+  delete g;
+  return MPS_OK;
+}
+
+int mps_graph_create(mps_ctx* c, mps_prog* const* progs, int n, mps_graph** out) {
+  if (!c || !out || n <= 0 || !progs) return fail(MPS_ERR_ARG, "bad argument");
+  *out = nullptr;
+  for (int i = 0; i < n; ++i) {
+    if (!progs[i] || progs[i]->ctx != c) return fail(MPS_ERR_ARG, "program from another context");
+    if (progs[i]->prec != progs[0]->prec) return fail(MPS_ERR_ARG, "batch mixes precisions");
+  }
+  std::lock_guard<std::mutex> lk(c->mu);
+  GCK(cudaSetDevice(c->device));
+  mps_graph* g = new mps_graph();
+  g->c = c;
+  g->progs.assign(progs, progs + n);
+  g->prec = progs[0]->prec;
+  int rc = lane_init(g->L);
+  if (rc) {
+    delete g;
+    return rc;
+  }
+  auto bail = [&](int code) {
+    mps_graph_destroy(g);
+    return code;
+  };
+  build_ops(g, g->flat, g->first, g->count);
+  // descriptors for every program (empty ones too: they still get reset),
+  // longest first
+  std::vector<int> order(n);
+  std::vector<double> cost(n, 0.0);
+  for (int i = 0; i < n; ++i) {
+    order[i] = i;
+    const double cap = (double)progs[i]->chi_cap;
+    for (size_t o = 0; o < g->count[i]; ++o)
+      cost[i] += (g->flat[g->first[i] + o].kind == OP_GATE2 ? 1.0 : 0.1) * cap * cap * cap;
+  }
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[a] > cost[b]; });
+  Lane& L = g->L;
+  if (cudaMalloc(&L.d_ops, std::max<size_t>(g->flat.size(), 1) * sizeof(DevOp)) != cudaSuccess ||
+      cudaMalloc(&L.d_desc, (size_t)n * sizeof(ProgDesc)) != cudaSuccess) {
+    cudaGetLastError();
+    return bail(fail(MPS_ERR_OOM, "graph op table allocation failed"));
+  }
+  L.d_ops_cap = std::max<size_t>(g->flat.size(), 1);
+  L.d_desc_cap = n;
+  std::vector<ProgDesc> descs;
+  for (int i : order) {
+    mps_prog* p = progs[i];
+    ProgDesc d;
+    std::memset(&d, 0, sizeof(d));
+    d.sites = p->d_sites;
+    d.site_off = p->d_off;
+    d.bond = p->d_bond;
+    d.ops = L.d_ops + g->first[i];
+    d.n_ops = (int)g->count[i];
+    d.n = p->n;
+    d.chi_cap = p->chi_cap;
+    d.mode = p->mode;
+    d.flags = p->flags;
+    d.cutoff = p->cutoff;
+    d.stats = p->d_stats;
+    d.err = p->d_err;
+    descs.push_back(d);
+  }
+  if (!g->flat.empty())
+    GCK(cudaMemcpy(L.d_ops, g->flat.data(), g->flat.size() * sizeof(DevOp), cudaMemcpyHostToDevice));
+  GCK(cudaMemcpy(L.d_desc, descs.data(), descs.size() * sizeof(ProgDesc), cudaMemcpyHostToDevice));
+  const int grid = std::min(n, c->num_sms);
+  const int prec = g->prec;
+  if (cudaMalloc(&L.op_scratch[prec], op_scratch_bytes(prec) * (size_t)grid) != cudaSuccess) {
+    cudaGetLastError();
+    return bail(fail(MPS_ERR_OOM, "graph scratch allocation failed"));
+  }
+  L.op_scratch_ctas[prec] = grid;
+  g->task_first.assign(n, (size_t)-1);
+  for (int i = 0; i < n; ++i)
+    if (progs[i]->d_obs) {
+      g->task_first[i] = g->tasks.size();
+      observable_tasks(progs[i], g->tasks);
+    }
+  const int nt = (int)g->tasks.size();
+  if (nt > 0) {
+    if (cudaMalloc(&L.exp_scratch[prec], expect_scratch_bytes(prec) * (size_t)nt) != cudaSuccess ||
+        cudaMalloc(&L.d_exp_tasks, (size_t)nt * sizeof(ExpTask)) != cudaSuccess ||
+        cudaMalloc(&L.d_exp_out, 2 * (size_t)nt * sizeof(double)) != cudaSuccess ||
+        cudaMallocHost(&g->h_out, 2 * (size_t)nt * sizeof(double)) != cudaSuccess) {
+      cudaGetLastError();
+      return bail(fail(MPS_ERR_OOM, "graph expectation buffers failed"));
+    }
+    L.exp_scratch_ctas[prec] = nt;
+    L.d_exp_tasks_cap = nt;
+    L.d_exp_out_cap = 2 * (size_t)nt;
+    GCK(cudaMemcpy(L.d_exp_tasks, g->tasks.data(), (size_t)nt * sizeof(ExpTask), cudaMemcpyHostToDevice));
+  }
+  cudaStream_t st = L.stream;
+  for (int i = 0; i < 3; ++i)
+    if (cudaEventCreate(&g->ev[i]) != cudaSuccess) return bail(fail(MPS_ERR_CUDA, "event creation failed"));
+  GCK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+  cudaError_t e = cudaEventRecord(g->ev[0], st);
+  if (e == cudaSuccess) e = launch_reset(prec, L.d_desc, n, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(L.d_queue, 0, sizeof(int), st);
+  if (e == cudaSuccess) e = launch_ops(prec, L.d_desc, n, grid, n > 1 ? L.d_queue : nullptr, L.op_scratch[prec], st);
+  if (e == cudaSuccess) e = cudaEventRecord(g->ev[1], st);
+  if (e == cudaSuccess && nt > 0) e = launch_expect(prec, L.d_exp_tasks, nt, L.exp_scratch[prec], L.d_exp_out, st);
+  if (e == cudaSuccess && nt > 0)
+    e = cudaMemcpyAsync(g->h_out, L.d_exp_out, 2 * (size_t)nt * sizeof(double), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaEventRecord(g->ev[2], st);
+  cudaGraph_t graph = nullptr;
+  const cudaError_t e2 = cudaStreamEndCapture(st, &graph);
+  if (e != cudaSuccess || e2 != cudaSuccess) {
+    if (graph) cudaGraphDestroy(graph);
+    return bail(fail(MPS_ERR_CUDA, cudaGetErrorString(e != cudaSuccess ? e : e2)));
+  }
+  g->graph = graph;
+  e = cudaGraphInstantiate(&g->exec, graph, 0);
+  if (e != cudaSuccess) return bail(fail(MPS_ERR_CUDA, cudaGetErrorString(e)));
+  *out = g;
+  return MPS_OK;
+}
+
+int mps_graph_update(mps_graph* g) {
+  if (!g) return fail(MPS_ERR_ARG, "NULL graph");
+  GCK(cudaSetDevice(g->c->device));
+  std::vector<DevOp> flat;
+  std::vector<size_t> first, count;
+  build_ops(g, flat, first, count);
+  if (count != g->count) return fail(MPS_ERR_ARG, "update changes the circuit structure");
+  for (size_t i = 0; i < flat.size(); ++i)
+    if (flat[i].kind != g->flat[i].kind || flat[i].site != g->flat[i].site || flat[i].orient != g->flat[i].orient)
+      return fail(MPS_ERR_ARG, "update changes the circuit structure");
+  g->flat.swap(flat);
+  if (!g->flat.empty())
+    GCK(cudaMemcpyAsync(g->L.d_ops, g->flat.data(), g->flat.size() * sizeof(DevOp), cudaMemcpyHostToDevice,
+                        g->L.stream));
+  return MPS_OK;
+}
+
+int mps_graph_launch_async(mps_graph* g) {
+  if (!g) return fail(MPS_ERR_ARG, "NULL graph");
+  GCK(cudaSetDevice(g->c->device));
+  GCK(cudaGraphLaunch(g->exec, g->L.stream));
+  for (mps_prog* p : g->progs) GCK(cudaEventRecord(p->ev, g->L.stream));
+  return MPS_OK;
+}
+
+int mps_graph_sync(mps_graph* g, double* energies) {
+  if (!g) return fail(MPS_ERR_ARG, "NULL graph");
+  GCK(cudaSetDevice(g->c->device));
+  GCK(cudaStreamSynchronize(g->L.stream));
+  for (size_t i = 0; i < g->progs.size(); ++i) {
+    int rc = prog_check_err(g->progs[i]);
+    if (rc) return rc;
+    if (energies)
+      energies[i] = g->task_first[i] == (size_t)-1 ? 0.0
+                                                   : observable_value(g->progs[i], g->h_out + 2 * g->task_first[i]);
+  }
+  return MPS_OK;
+}
+
+int mps_graph_launch(mps_graph* g, double* energies) {
+  int rc = mps_graph_launch_async(g);
+  if (rc) return rc;
+  return mps_graph_sync(g, energies);
+}
+
+int mps_graph_timing(mps_graph* g, double out[4]) {
+  if (!g || !out) return fail(MPS_ERR_ARG, "NULL argument");
+  GCK(cudaSetDevice(g->c->device));
+  GCK(cudaStreamSynchronize(g->L.stream));
+  float a = 0.f, b = 0.f;
+  GCK(cudaEventElapsedTime(&a, g->ev[0], g->ev[1]));
+  GCK(cudaEventElapsedTime(&b, g->ev[1], g->ev[2]));
+  out[0] = a;
+  out[1] = b;
+  double fl = 0.0, ef = 0.0;
+  for (mps_prog* p : g->progs) {
+    double st[ST_COUNT];
+    GCK(cudaMemcpy(st, p->d_stats, sizeof(st), cudaMemcpyDeviceToHost));
+    fl += st[ST_FLOPS];
+    ef += st[ST_EIG_FLOPS];
+  }
+  out[2] = fl;
+  out[3] = ef;
+  return MPS_OK;
+}
+
+int mps_graph_stream(mps_graph* g, void** s) {
+  if (!g || !s) return fail(MPS_ERR_ARG, "NULL argument");
+  *s = (void*)g->L.stream;
+  return MPS_OK;
+}
+
+}  // extern "C"

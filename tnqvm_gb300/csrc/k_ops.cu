@@ -1,0 +1,671 @@
+// Fused single-CTA MPS update kernels (sm_103a).
+//
+// One CTA executes one program's op list in order: single-site gates
+// (ExaTnMpsVisitor.cpp:1185-1292, ITensorMPSVisitor.cpp:288-299), two-site
+// gates with SVD split and truncation (ExaTnMpsVisitor.cpp:1387-1730 +
+// truncateSvdTensors :2366-2536; ITensorMPSVisitor.cpp:312-331 + ITensor
+// truncate decomp.cc:307-463), and orthogonality-centre moves (ITensor
+// MPS::position, ITensorMPSVisitor.cpp:294,317).  The persistent launch pulls
+// programs from an atomic queue, so a batch of circuits of any size runs in
+// one launch with no inter-CTA waits.
+//
+// Two-site split: theta = gate . (A . B) is formed in per-CTA scratch, its
+// Gram matrix on the isometric side is diagonalised by a parallel cyclic
+// Jacobi method (round-robin pairs, all m/2 rotations of a step applied at
+// once as 2x2 block updates), the eigenvalues (squared singular values) are
+// sorted, the kept dimension is chosen with FP64 sums, and the other side is
+// the projection W_k^H X (no division by singular values).
+#include <math.h>
+
+#include "mps_common.cuh"
+
+namespace gbmps {
+
+template <typename T>
+struct Prec;
+template <>
+struct Prec<float> {
+  static constexpr double eps = 1.1920929e-07;
+  static constexpr bool u_in_smem = true;
+  static constexpr int max_sweeps = 24;
+};
+template <>
+struct Prec<double> {
+  static constexpr double eps = 2.220446049250313e-16;
+  static constexpr bool u_in_smem = false;
+  static constexpr int max_sweeps = 30;
+};
+
+__device__ __forceinline__ int pidx(int i, int j, int m) {  // i <= j
+  return i * m - ((i * (i - 1)) >> 1) + (j - i);
+}
+
+template <typename T>
+__device__ __forceinline__ cx<T> gget(const cx<T>* Gp, int i, int j, int m) {
+  return i <= j ? Gp[pidx(i, j, m)] : conj(Gp[pidx(j, i, m)]);
+}
+template <typename T>
+__device__ __forceinline__ void gset(cx<T>* Gp, int i, int j, int m, cx<T> v) {
+  if (i <= j)
+    Gp[pidx(i, j, m)] = v;
+  else
+    Gp[pidx(j, i, m)] = conj(v);
+}
+
+__device__ __forceinline__ void rr_pair(int m, int r, int j, int& p, int& q) {
+  if (j == 0) {
+    p = m - 1;
+    q = r;
+  } else {
+    p = (r + j) % (m - 1);
+    q = (r - j + m - 1) % (m - 1);
+  }
+}
+
+// Block-wide sum of a double; `red` holds >= 32 doubles of shared memory.
+__device__ double block_sum(double v, double* red) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) red[w] = v;
+  __syncthreads();
+  double s = 0.0;
+  const int nw = blockDim.x >> 5;
+  for (int i = 0; i < nw; ++i) s += red[i];
+  __syncthreads();
+  return s;
+}
+
+// Small per-CTA shared state that lives after the large arrays.
+template <typename T>
+struct SmallSmem {
+  double lam[kMaxM];
+  int perm[kMaxM];
+  T iso[kMaxM];
+  T oth[kMaxM];
+  int rp_p[kMaxM / 2], rp_q[kMaxM / 2], rp_on[kMaxM / 2];
+  T rp_c[kMaxM / 2], rp_s[kMaxM / 2], rp_er[kMaxM / 2], rp_ei[kMaxM / 2];
+  cx<T> g[16];
+  cx<T> tau[kChiLimit];
+  double red[32];
+  int ival[8];
+  double dval[8];
+};
+
+template <typename T>
+struct Layout {
+  // Large shared region: Gram (packed upper) [+ U for FP32], or the QR matrix + R.
+  static constexpr size_t gram_bytes = sizeof(cx<T>) * (kMaxM * (kMaxM + 1) / 2);
+  static constexpr size_t u_bytes = Prec<T>::u_in_smem ? sizeof(cx<T>) * kMaxM * kMaxM : 0;
+  static constexpr size_t qr_bytes = sizeof(cx<T>) * (kMaxM * kChiLimit + kChiLimit * kChiLimit);
+  static constexpr size_t big = (gram_bytes + u_bytes) > qr_bytes ? (gram_bytes + u_bytes) : qr_bytes;
+  static constexpr size_t smem = big + sizeof(SmallSmem<T>);
+  // Global scratch per CTA: theta, and U for FP64.
+  static constexpr size_t scratch = sizeof(cx<T>) * kMaxM * kMaxM * (Prec<T>::u_in_smem ? 1 : 2);
+};
+
+// ------------------------------------------------------------------ Jacobi
+// Diagonalise the m x m Hermitian matrix held packed in Gp; U (ld = m)
+// receives the eigenvectors as columns; eigenvalues are left on the diagonal.
+template <typename T>
+__device__ int jacobi_eigh(cx<T>* Gp, cx<T>* U, int m, double trace, SmallSmem<T>* sm) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  int total_rot = 0;
+  for (int t = tid; t < m * m; t += nt) {
+    const int i = t / m, j = t - i * m;
+    U[t] = mk<T>(i == j ? T(1) : T(0), T(0));
+  }
+  __syncthreads();
+  const int np = m >> 1;
+  const T tol_rel = T(Prec<T>::eps);
+  const T tol_abs = T(Prec<T>::eps * trace);
+  for (int sweep = 0; sweep < Prec<T>::max_sweeps; ++sweep) {
+    if (tid == 0) sm->ival[0] = 0;
+    __syncthreads();
+    for (int r = 0; r < m - 1; ++r) {
+      for (int j = tid; j < np; j += nt) {
+        int p, q;
+        rr_pair(m, r, j, p, q);
+        const T a = Gp[pidx(p, p, m)].re, b = Gp[pidx(q, q, m)].re;
+        const cx<T> g = gget(Gp, p, q, m);
+        const T ag = sqrt(abs2(g));
+        int on = 0;
+        T c = T(1), s = T(0), er = T(1), ei = T(0);
+        if (ag > tol_abs && ag > tol_rel * sqrt(fabs(a * b))) {
+          on = 1;
+          er = g.re / ag;
+          ei = g.im / ag;
+          const T zeta = (b - a) / (T(2) * ag);
+          const T tt = (zeta >= T(0) ? T(1) : T(-1)) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
+          c = T(1) / sqrt(T(1) + tt * tt);
+          s = c * tt;
+          atomicAdd(&sm->ival[0], 1);
+        }
+        sm->rp_p[j] = p;
+        sm->rp_q[j] = q;
+        sm->rp_on[j] = on;
+        sm->rp_c[j] = c;
+        sm->rp_s[j] = s;
+        sm->rp_er[j] = er;
+        sm->rp_ei[j] = ei;
+      }
+      __syncthreads();
+      // G <- J^H G J as independent 2x2 block updates over pair blocks I <= J.
+      for (int t = tid; t < np * np; t += nt) {
+        const int I = t / np, J = t - I * np;
+        if (I > J) continue;
+        const int onI = sm->rp_on[I], onJ = sm->rp_on[J];
+        if (!onI && !onJ) continue;
+        const int pI = sm->rp_p[I], qI = sm->rp_q[I], pJ = sm->rp_p[J], qJ = sm->rp_q[J];
+        // J = [[c, s], [-s e*, c e*]]
+        cx<T> jI00 = mk<T>(sm->rp_c[I], 0), jI01 = mk<T>(sm->rp_s[I], 0);
+        cx<T> eIc = mk<T>(sm->rp_er[I], -sm->rp_ei[I]);
+        cx<T> jI10 = scl(eIc, -sm->rp_s[I]), jI11 = scl(eIc, sm->rp_c[I]);
+        cx<T> jJ00 = mk<T>(sm->rp_c[J], 0), jJ01 = mk<T>(sm->rp_s[J], 0);
+        cx<T> eJc = mk<T>(sm->rp_er[J], -sm->rp_ei[J]);
+        cx<T> jJ10 = scl(eJc, -sm->rp_s[J]), jJ11 = scl(eJc, sm->rp_c[J]);
+        if (I == J) {
+          const T a = Gp[pidx(pI, pI, m)].re, b = Gp[pidx(qI, qI, m)].re;
+          const cx<T> g = gget(Gp, pI, qI, m);
+          // diag(J^H B J): a' = |j00|^2 a + |j10|^2 b + 2 Re(conj(j00) g j10)
+          const cx<T> x = conj(jI00) * g * jI10;
+          const cx<T> y = conj(jI01) * g * jI11;
+          const T an = abs2(jI00) * a + abs2(jI10) * b + T(2) * x.re;
+          const T bn = abs2(jI01) * a + abs2(jI11) * b + T(2) * y.re;
+          Gp[pidx(pI, pI, m)] = mk<T>(an, 0);
+          Gp[pidx(qI, qI, m)] = mk<T>(bn, 0);
+          gset(Gp, pI, qI, m, mk<T>(0, 0));
+          continue;
+        }
+        const cx<T> b00 = gget(Gp, pI, pJ, m), b01 = gget(Gp, pI, qJ, m);
+        const cx<T> b10 = gget(Gp, qI, pJ, m), b11 = gget(Gp, qI, qJ, m);
+        cx<T> c00 = b00, c01 = b01, c10 = b10, c11 = b11;
+        if (onJ) {  // B J
+          c00 = b00 * jJ00 + b01 * jJ10;
+          c01 = b00 * jJ01 + b01 * jJ11;
+          c10 = b10 * jJ00 + b11 * jJ10;
+          c11 = b10 * jJ01 + b11 * jJ11;
+        }
+        cx<T> d00 = c00, d01 = c01, d10 = c10, d11 = c11;
+        if (onI) {  // J^H (B J)
+          d00 = conj(jI00) * c00 + conj(jI10) * c10;
+          d01 = conj(jI00) * c01 + conj(jI10) * c11;
+          d10 = conj(jI01) * c00 + conj(jI11) * c10;
+          d11 = conj(jI01) * c01 + conj(jI11) * c11;
+        }
+        gset(Gp, pI, pJ, m, d00);
+        gset(Gp, pI, qJ, m, d01);
+        gset(Gp, qI, pJ, m, d10);
+        gset(Gp, qI, qJ, m, d11);
+      }
+      // U <- U J
+      for (int t = tid; t < m * np; t += nt) {
+        const int row = t / np, j = t - row * np;
+        if (!sm->rp_on[j]) continue;
+        const int p = sm->rp_p[j], q = sm->rp_q[j];
+        const T c = sm->rp_c[j], s = sm->rp_s[j];
+        const cx<T> ec = mk<T>(sm->rp_er[j], -sm->rp_ei[j]);
+        const cx<T> up = U[row * m + p], uq = U[row * m + q];
+        const cx<T> uqe = uq * ec;
+        U[row * m + p] = scl(up, c) - scl(uqe, s);
+        U[row * m + q] = scl(up, s) + scl(uqe, c);
+      }
+      __syncthreads();
+    }
+    const int nrot = sm->ival[0];
+    __syncthreads();
+    total_rot += nrot;
+    if (nrot == 0) break;
+  }
+  return total_rot;
+}
+
+// ---------------------------------------------------------- Householder QR
+// M (mr x nc, ld = nc) -> Q in the first k = min(mr,nc) columns of M,
+// R (k x nc, ld = nc) in Rb.  Same reflector convention as LAPACK zgeqr2/zung2r.
+template <typename T>
+__device__ void householder_qr(cx<T>* M, int mr, int nc, cx<T>* Rb, SmallSmem<T>* sm) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+  const int k = mr < nc ? mr : nc;
+  for (int j = 0; j < k; ++j) {
+    double s = 0.0;
+    for (int i = j + 1 + tid; i < mr; i += nt) s += (double)abs2(M[i * nc + j]);
+    s = block_sum(s, sm->red);
+    if (tid == 0) {
+      const cx<T> alpha = M[j * nc + j];
+      const double ar = alpha.re, ai = alpha.im;
+      if (s == 0.0 && ai == 0.0) {
+        sm->tau[j] = mk<T>(0, 0);
+        sm->ival[1] = 0;
+      } else {
+        const double beta = -copysign(sqrt(ar * ar + ai * ai + s), ar);
+        sm->tau[j] = mk<T>(T((beta - ar) / beta), T(-ai / beta));
+        // 1 / (alpha - beta)
+        const double dr = ar - beta, di = ai, den = dr * dr + di * di;
+        sm->dval[0] = dr / den;
+        sm->dval[1] = -di / den;
+        M[j * nc + j] = mk<T>(T(beta), T(0));
+        sm->ival[1] = 1;
+      }
+    }
+    __syncthreads();
+    if (sm->ival[1]) {
+      const cx<T> inv = mk<T>(T(sm->dval[0]), T(sm->dval[1]));
+      for (int i = j + 1 + tid; i < mr; i += nt) M[i * nc + j] = M[i * nc + j] * inv;
+      __syncthreads();
+      const cx<T> ctau = conj(sm->tau[j]);
+      for (int c = j + 1 + warp; c < nc; c += nw) {
+        cx<T> w = mk<T>(0, 0);
+        for (int i = j + 1 + lane; i < mr; i += 32) fma_cj(w, M[i * nc + j], M[i * nc + c]);
+        for (int o = 16; o > 0; o >>= 1) {
+          w.re += __shfl_xor_sync(0xffffffffu, w.re, o);
+          w.im += __shfl_xor_sync(0xffffffffu, w.im, o);
+        }
+        w = w + M[j * nc + c];
+        const cx<T> tw = ctau * w;
+        for (int i = j + 1 + lane; i < mr; i += 32) M[i * nc + c] = M[i * nc + c] - M[i * nc + j] * tw;
+        __syncwarp();
+        if (lane == 0) M[j * nc + c] = M[j * nc + c] - tw;
+      }
+    }
+    __syncthreads();
+  }
+  for (int t = tid; t < k * nc; t += nt) {
+    const int i = t / nc, c = t - i * nc;
+    Rb[t] = c >= i ? M[i * nc + c] : mk<T>(0, 0);
+  }
+  __syncthreads();
+  for (int j = k - 1; j >= 0; --j) {
+    const cx<T> tj = sm->tau[j];
+    if (j < k - 1 && (tj.re != T(0) || tj.im != T(0))) {
+      for (int c = j + 1 + warp; c < k; c += nw) {
+        cx<T> w = mk<T>(0, 0);
+        for (int i = j + 1 + lane; i < mr; i += 32) fma_cj(w, M[i * nc + j], M[i * nc + c]);
+        for (int o = 16; o > 0; o >>= 1) {
+          w.re += __shfl_xor_sync(0xffffffffu, w.re, o);
+          w.im += __shfl_xor_sync(0xffffffffu, w.im, o);
+        }
+        w = w + M[j * nc + c];
+        const cx<T> tw = tj * w;
+        for (int i = j + 1 + lane; i < mr; i += 32) M[i * nc + c] = M[i * nc + c] - M[i * nc + j] * tw;
+        __syncwarp();
+        if (lane == 0) M[j * nc + c] = M[j * nc + c] - tw;
+      }
+    }
+    __syncthreads();
+    for (int i = tid; i < mr; i += nt) {
+      if (i > j)
+        M[i * nc + j] = mk<T>(T(0), T(0)) - tj * M[i * nc + j];
+      else if (i == j)
+        M[i * nc + j] = mk<T>(T(1) - tj.re, -tj.im);
+      else
+        M[i * nc + j] = mk<T>(0, 0);
+    }
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------------------- ops
+template <typename T>
+__device__ void op_gate1(const ProgDesc& P, const DevOp& op, SmallSmem<T>* sm) {
+  const int s = op.site;
+  cx<T>* A = reinterpret_cast<cx<T>*>(P.sites) + P.site_off[s];
+  const int dl = P.bond[s], dr = P.bond[s + 1];
+  const cx<T> g00 = mk<T>(T(op.m[0]), T(op.m[1])), g01 = mk<T>(T(op.m[2]), T(op.m[3]));
+  const cx<T> g10 = mk<T>(T(op.m[4]), T(op.m[5])), g11 = mk<T>(T(op.m[6]), T(op.m[7]));
+  for (int idx = threadIdx.x; idx < dl * dr; idx += blockDim.x) {
+    const int l = idx / dr, r = idx - l * dr;
+    const cx<T> a0 = A[(l * 2) * dr + r], a1 = A[(l * 2 + 1) * dr + r];
+    A[(l * 2) * dr + r] = g00 * a0 + g01 * a1;
+    A[(l * 2 + 1) * dr + r] = g10 * a0 + g11 * a1;
+  }
+}
+
+template <typename T>
+__device__ void op_gate2(const ProgDesc& P, const DevOp& op, char* big, SmallSmem<T>* sm, char* scratch) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int lo = op.site;
+  const int dl = P.bond[lo], dm = P.bond[lo + 1], dr = P.bond[lo + 2];
+  if (dl > kChiLimit || dm > kChiLimit || dr > kChiLimit) {
+    if (tid == 0) atomicOr(P.err, ERR_DIMS);
+    return;
+  }
+  cx<T>* sites = reinterpret_cast<cx<T>*>(P.sites);
+  cx<T>* A = sites + P.site_off[lo];
+  cx<T>* B = sites + P.site_off[lo + 1];
+  const int R = 2 * dl, Cc = 2 * dr;
+  cx<T>* Th = reinterpret_cast<cx<T>*>(scratch);
+  if (tid < 16) sm->g[tid] = mk<T>(T(op.m[2 * tid]), T(op.m[2 * tid + 1]));
+  __syncthreads();
+  // theta[(l,p1),(p2,r)] = sum_{q1,q2} G[2p1+p2][2q1+q2] sum_m A[l,q1,m] B[m,q2,r]
+  for (int idx = tid; idx < dl * dr; idx += nt) {
+    const int l = idx / dr, r = idx - l * dr;
+    cx<T> t[4] = {mk<T>(0, 0), mk<T>(0, 0), mk<T>(0, 0), mk<T>(0, 0)};
+    const cx<T>* a0 = A + (l * 2) * dm;
+    const cx<T>* a1 = a0 + dm;
+    for (int mm = 0; mm < dm; ++mm) {
+      const cx<T> x0 = a0[mm], x1 = a1[mm];
+      const cx<T> y0 = B[(mm * 2) * dr + r], y1 = B[(mm * 2 + 1) * dr + r];
+      fma_c(t[0], x0, y0);
+      fma_c(t[1], x0, y1);
+      fma_c(t[2], x1, y0);
+      fma_c(t[3], x1, y1);
+    }
+#pragma unroll
+    for (int row = 0; row < 4; ++row) {
+      cx<T> acc = mk<T>(0, 0);
+#pragma unroll
+      for (int col = 0; col < 4; ++col) fma_c(acc, sm->g[row * 4 + col], t[col]);
+      Th[(l * 2 + (row >> 1)) * Cc + (row & 1) * dr + r] = acc;
+    }
+  }
+  __syncthreads();
+  // Isometric side: rows of theta (tr = false) or its columns (tr = true).
+  bool tr;
+  if (op.orient == ORIENT_TO_HI)
+    tr = false;
+  else if (op.orient == ORIENT_TO_LO)
+    tr = true;
+  else
+    tr = R > Cc;
+  const int m = tr ? Cc : R, nn = tr ? R : Cc;
+  auto X = [&](int i, int c) -> cx<T> { return tr ? Th[c * Cc + i] : Th[i * Cc + c]; };
+  cx<T>* Gp = reinterpret_cast<cx<T>*>(big);
+  cx<T>* U = Prec<T>::u_in_smem ? reinterpret_cast<cx<T>*>(big + Layout<T>::gram_bytes)
+                                : reinterpret_cast<cx<T>*>(scratch + sizeof(cx<T>) * kMaxM * kMaxM);
+  double tr_part = 0.0;
+  for (int t = tid; t < m * m; t += nt) {
+    const int i = t / m, j = t - i * m;
+    if (i > j) continue;
+    cx<T> acc = mk<T>(0, 0);
+    for (int c = 0; c < nn; ++c) fma_c(acc, X(i, c), conj(X(j, c)));
+    if (i == j) {
+      acc.im = T(0);
+      tr_part += (double)acc.re;
+    }
+    Gp[pidx(i, j, m)] = acc;
+  }
+  const double trace = block_sum(tr_part, sm->red);
+  const int nrot_total = jacobi_eigh<T>(Gp, U, m, trace, sm);
+  // eigenvalues, descending order
+  for (int i = tid; i < m; i += nt) sm->lam[i] = (double)Gp[pidx(i, i, m)].re;
+  __syncthreads();
+  for (int i = tid; i < m; i += nt) {
+    const double li = sm->lam[i];
+    int rank = 0;
+    for (int j = 0; j < m; ++j) {
+      const double lj = sm->lam[j];
+      rank += (lj > li) || (lj == li && j < i);
+    }
+    sm->perm[rank] = i;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    const int mm = R < Cc ? R : Cc;  // number of singular values (min(vol) in ExaTnMpsVisitor.cpp:1594)
+    double total = 0.0;
+    int bad = 0;
+    for (int i = 0; i < mm; ++i) {
+      const double v = sm->lam[sm->perm[i]];
+      if (!(v == v) || isinf(v)) bad = 1;
+      total += v > 0.0 ? v : 0.0;
+    }
+    int k = mm;
+    const int cap = P.chi_cap;
+    if (P.mode == TRUNC_EXATN) {
+      // first index whose partial norms (= singular value) are below the cutoff, keep it too
+      for (int i = 0; i < mm; ++i) {
+        const double v = sm->lam[sm->perm[i]];
+        const double sv = v > 0.0 ? sqrt(v) : 0.0;
+        if (sv < P.cutoff) {
+          k = i + 1;
+          break;
+        }
+      }
+      if (k > cap) k = cap;
+    } else {
+      // ITensor truncate (decomp.cc:307-463), relative cutoff, mindim 1
+      const double p0 = sm->lam[sm->perm[0]];
+      if (!(p0 > 0.0) || mm == 1) {
+        k = 1;
+      } else {
+        double scale = 0.0;
+        for (int i = 0; i < mm; ++i) {
+          const double v = sm->lam[sm->perm[i]] / p0;
+          scale += v > 0.0 ? v : 0.0;
+        }
+        int n = mm - 1;
+        double err = 0.0;
+        while (n >= cap) {
+          const double v = sm->lam[sm->perm[n]] / p0;
+          err += v > 0.0 ? v : 0.0;
+          --n;
+        }
+        if (scale == 0.0) scale = 1.0;
+        while (n >= 1) {
+          const double v = sm->lam[sm->perm[n]] / p0;
+          const double pv = v > 0.0 ? v : 0.0;
+          if (err + pv > P.cutoff * scale) break;
+          err += pv;
+          --n;
+        }
+        k = n + 1;
+      }
+    }
+    if (k < 1) k = 1;
+    double kept = 0.0;
+    for (int i = 0; i < k; ++i) {
+      const double v = sm->lam[sm->perm[i]];
+      kept += v > 0.0 ? v : 0.0;
+    }
+    const double frac = total > 0.0 ? (total - kept) / total : 0.0;
+    double rn = 1.0;
+    if ((P.flags & 1) && kept > 0.0) rn = sqrt(total / kept);
+    sm->ival[2] = k;
+    sm->dval[2] = rn;
+    P.stats[ST_LOG_FID] += log1p(-(frac < 1.0 ? frac : 0.0));
+    if (frac > P.stats[ST_MAX_DISC]) P.stats[ST_MAX_DISC] = frac;
+    P.stats[ST_N_GATE2] += 1.0;
+    // algorithmic flops (complex MAC = 8): merge, gate, Gram, split
+    P.stats[ST_FLOPS] += 32.0 * dl * dm * dr + 128.0 * dl * dr + 8.0 * m * m * nn + 8.0 * k * nn * m;
+    // each rotation updates two rows and two columns of G and two columns of U
+    P.stats[ST_EIG_FLOPS] += 96.0 * m * nrot_total;
+    if (bad) atomicOr(P.err, ERR_NAN);
+  }
+  __syncthreads();
+  const int k = sm->ival[2];
+  const double rn = sm->dval[2];
+  for (int j = tid; j < k; j += nt) {
+    const double v = sm->lam[sm->perm[j]];
+    const double sv = v > 0.0 ? sqrt(v) : 0.0;
+    if (op.orient == ORIENT_SQRT) {
+      const double h = sqrt(sv);
+      sm->iso[j] = T(h);
+      sm->oth[j] = T(h > 0.0 ? rn / h : 0.0);
+    } else {
+      sm->iso[j] = T(1);
+      sm->oth[j] = T(rn);
+    }
+  }
+  __syncthreads();
+  // other side: Z = W_k^H X (k x nn)
+  for (int t = tid; t < k * nn; t += nt) {
+    const int j = t / nn, c = t - j * nn;
+    const int pj = sm->perm[j];
+    cx<T> acc = mk<T>(0, 0);
+    for (int i = 0; i < m; ++i) fma_cj(acc, U[i * m + pj], X(i, c));
+    acc = scl(acc, sm->oth[j]);
+    if (!tr)
+      B[j * Cc + c] = acc;  // hi site (k, 2, dr)
+    else
+      A[c * k + j] = acc;   // lo site (dl, 2, k)
+  }
+  // isometric side: W_k
+  for (int t = tid; t < m * k; t += nt) {
+    const int i = t / k, j = t - i * k;
+    const cx<T> w = scl(U[i * m + sm->perm[j]], sm->iso[j]);
+    if (!tr)
+      A[i * k + j] = w;   // lo site (dl, 2, k)
+    else
+      B[j * Cc + i] = w;  // hi site (k, 2, dr)
+  }
+  __syncthreads();
+  if (tid == 0) P.bond[lo + 1] = k;
+}
+
+// Centre move to the right: A_c = Q R (rows (l,p)), A_{c+1} <- R A_{c+1}.
+template <typename T>
+__device__ void op_move_r(const ProgDesc& P, const DevOp& op, char* big, SmallSmem<T>* sm, char* scratch) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int c = op.site;
+  const int dl = P.bond[c], dr = P.bond[c + 1], dr2 = P.bond[c + 2];
+  if (2 * dl > kMaxM || dr > kChiLimit) {
+    if (tid == 0) atomicOr(P.err, ERR_DIMS);
+    return;
+  }
+  cx<T>* sites = reinterpret_cast<cx<T>*>(P.sites);
+  cx<T>* A = sites + P.site_off[c];
+  cx<T>* B = sites + P.site_off[c + 1];
+  cx<T>* M = reinterpret_cast<cx<T>*>(big);
+  cx<T>* Rb = M + kMaxM * kChiLimit;
+  const int mr = 2 * dl, nc = dr;
+  for (int t = tid; t < mr * nc; t += nt) M[t] = A[t];
+  __syncthreads();
+  householder_qr<T>(M, mr, nc, Rb, sm);
+  const int k = mr < nc ? mr : nc;
+  for (int t = tid; t < mr * k; t += nt) {
+    const int i = t / k, j = t - i * k;
+    A[t] = M[i * nc + j];
+  }
+  cx<T>* out = reinterpret_cast<cx<T>*>(scratch);
+  const int w = 2 * dr2;
+  for (int t = tid; t < k * w; t += nt) {
+    const int i = t / w, x = t - i * w;
+    cx<T> acc = mk<T>(0, 0);
+    for (int j = i; j < nc; ++j) fma_c(acc, Rb[i * nc + j], B[j * w + x]);
+    out[t] = acc;
+  }
+  __syncthreads();
+  for (int t = tid; t < k * w; t += nt) B[t] = out[t];
+  __syncthreads();
+  if (tid == 0) {
+    P.bond[c + 1] = k;
+    P.stats[ST_FLOPS] += 4.0 * k * nc * w;
+    P.stats[ST_EIG_FLOPS] += 32.0 * mr * nc * nc;
+  }
+}
+
+// Centre move to the left: A_c^H = Q R, A_c <- Q^H, A_{c-1} <- A_{c-1} R^H.
+template <typename T>
+__device__ void op_move_l(const ProgDesc& P, const DevOp& op, char* big, SmallSmem<T>* sm, char* scratch) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int c = op.site;
+  const int dl = P.bond[c], dr = P.bond[c + 1], dl2 = P.bond[c - 1];
+  if (2 * dr > kMaxM || dl > kChiLimit) {
+    if (tid == 0) atomicOr(P.err, ERR_DIMS);
+    return;
+  }
+  cx<T>* sites = reinterpret_cast<cx<T>*>(P.sites);
+  cx<T>* A = sites + P.site_off[c];
+  cx<T>* L = sites + P.site_off[c - 1];
+  cx<T>* M = reinterpret_cast<cx<T>*>(big);
+  cx<T>* Rb = M + kMaxM * kChiLimit;
+  const int mr = 2 * dr, nc = dl;
+  for (int t = tid; t < mr * nc; t += nt) {
+    const int i = t / nc, j = t - i * nc;
+    M[t] = conj(A[j * mr + i]);
+  }
+  __syncthreads();
+  householder_qr<T>(M, mr, nc, Rb, sm);
+  const int k = mr < nc ? mr : nc;
+  for (int t = tid; t < k * mr; t += nt) {
+    const int j = t / mr, i = t - j * mr;
+    A[t] = conj(M[i * nc + j]);
+  }
+  cx<T>* out = reinterpret_cast<cx<T>*>(scratch);
+  const int h = 2 * dl2;
+  for (int t = tid; t < h * k; t += nt) {
+    const int x = t / k, j = t - x * k;
+    cx<T> acc = mk<T>(0, 0);
+    for (int i = j; i < nc; ++i) fma_cj(acc, Rb[j * nc + i], L[x * nc + i]);  // sum_i L[x,i] conj(R[j,i])
+    out[t] = acc;
+  }
+  __syncthreads();
+  for (int t = tid; t < h * k; t += nt) L[t] = out[t];
+  __syncthreads();
+  if (tid == 0) {
+    P.bond[c] = k;
+    P.stats[ST_FLOPS] += 4.0 * k * nc * h;
+    P.stats[ST_EIG_FLOPS] += 32.0 * mr * nc * nc;
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kOpThreads, 1)
+k_run_ops(const ProgDesc* __restrict__ progs, int n_progs, int* queue, char* scratch_base, size_t scratch_stride) {
+  extern __shared__ __align__(16) char smem[];
+  char* big = smem;
+  SmallSmem<T>* sm = reinterpret_cast<SmallSmem<T>*>(smem + Layout<T>::big);
+  char* scratch = scratch_base + scratch_stride * blockIdx.x;
+  int pi = blockIdx.x;
+  while (true) {
+    if (queue != nullptr) {
+      if (threadIdx.x == 0) sm->ival[7] = atomicAdd(queue, 1);
+      __syncthreads();
+      pi = sm->ival[7];
+      __syncthreads();
+    }
+    if (pi >= n_progs) break;
+    const ProgDesc P = progs[pi];
+    for (int o = 0; o < P.n_ops; ++o) {
+      const DevOp& op = P.ops[o];
+      switch (op.kind) {
+        case OP_GATE1:
+          op_gate1<T>(P, op, sm);
+          break;
+        case OP_GATE2:
+          op_gate2<T>(P, op, big, sm, scratch);
+          break;
+        case OP_MOVE_R:
+          op_move_r<T>(P, op, big, sm, scratch);
+          break;
+        case OP_MOVE_L:
+          op_move_l<T>(P, op, big, sm, scratch);
+          break;
+        default:
+          break;
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) P.stats[ST_N_OPS] += (double)P.n_ops;
+    if (queue == nullptr) break;
+  }
+}
+
+// ------------------------------------------------------------- launchers
+template <typename T>
+static cudaError_t launch_ops_t(const ProgDesc* d_progs, int n_progs, int grid, int* d_queue, char* scratch,
+                                cudaStream_t st) {
+  k_run_ops<T><<<grid, kOpThreads, Layout<T>::smem, st>>>(d_progs, n_progs, d_queue, scratch, Layout<T>::scratch);
+  return cudaGetLastError();
+}
+
+// Opt in to the large dynamic shared memory once per device (outside any capture).
+cudaError_t configure_ops() {
+  cudaError_t e = cudaFuncSetAttribute(k_run_ops<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)Layout<float>::smem);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_run_ops<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)Layout<double>::smem);
+}
+
+size_t op_scratch_bytes(int prec) { return prec == 0 ? Layout<double>::scratch : Layout<float>::scratch; }
+size_t op_smem_bytes(int prec) { return prec == 0 ? Layout<double>::smem : Layout<float>::smem; }
+
+cudaError_t launch_ops(int prec, const ProgDesc* d_progs, int n_progs, int grid, int* d_queue, char* scratch,
+                       cudaStream_t st) {
+  if (prec == 0) return launch_ops_t<double>(d_progs, n_progs, grid, d_queue, scratch, st);
+  return launch_ops_t<float>(d_progs, n_progs, grid, d_queue, scratch, st);
+}
+
+}  // namespace gbmps

@@ -1,0 +1,277 @@
+// Continuous-batching request loop of the GB300 MPS engine.
+//
+// A worker thread owns several lanes (stream + scratch).  Requests (programs
+// with recorded gates, an optional observable and a shot count) queue up in
+// arrival order; whenever a lane is free the worker admits as many queued
+// requests as the in-flight request cap and the HBM footprint budget allow,
+// launches them as one persistent batch on that lane, enqueues the batch's
+// expectation and sampling work behind it, and records an event.  Batches on
+// different lanes overlap on the device, so requests that arrive while others
+// run start as soon as a lane is free instead of waiting for the running
+// batch to drain.  Completed requests are finished out of order.
+#include <chrono>
+#include <cstring>
+
+#include "../../include/gb300mps.h"
+#include "engine_internal.hpp"
+
+namespace gbmps {
+
+constexpr int kServeLanes = 4;
+
+static double now_ms() {
+  return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+static int grow_pinned(void** p, size_t* cap, size_t need) {
+  if (*cap >= need) return MPS_OK;
+  if (*p) cudaFreeHost(*p);
+  *p = nullptr;
+  *cap = 0;
+  const size_t n = need + need / 2 + 256;
+  if (cudaMallocHost(p, n) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(MPS_ERR_OOM, "pinned host allocation failed");
+  }
+  *cap = n;
+  return MPS_OK;
+}
+
+static void finish_batch(ServeState* S, ServeBatch& B) {
+  const double t = now_ms();
+  std::lock_guard<std::mutex> lk(S->mu);
+  size_t ti = 0;
+  for (ServeReq* r : B.reqs) {
+    mps_prog* p = r->prog;
+    r->status = prog_check_err(p);
+    if (p->d_obs) {
+      r->energy = observable_value(p, B.h_exp + 2 * ti);
+      ti += (size_t)p->n_terms + 1;
+    }
+    r->t_done = t;
+    r->done = true;
+  }
+  for (auto& bd : B.bit_dst) {
+    ServeReq* r = bd.first;
+    select_measured(r->prog, bd.second, r->shots, r->bits.data());
+  }
+  S->inflight_bytes -= B.footprint;
+  S->inflight_reqs -= (int)B.reqs.size();
+  B.reqs.clear();
+  B.bit_dst.clear();
+  S->cv_done.notify_all();
+}
+
+static int launch_batch(mps_ctx* c, ServeState* S, int li, std::vector<ServeReq*>& reqs) {
+  Lane& L = S->lanes[li];
+  ServeBatch& B = S->batches[li];
+  B.reqs = reqs;
+  B.footprint = 0;
+  std::vector<mps_prog*> progs;
+  progs.reserve(reqs.size());
+  for (ServeReq* r : reqs) {
+    progs.push_back(r->prog);
+    B.footprint += r->prog->bytes;
+  }
+  int rc = launch_programs(c, L, progs.data(), (int)progs.size(), false);
+  if (rc) return rc;
+  B.tasks.clear();
+  int prec = progs[0]->prec;
+  for (mps_prog* p : progs)
+    if (p->d_obs) observable_tasks(p, B.tasks);
+  if (!B.tasks.empty()) {
+    rc = grow_pinned((void**)&B.h_exp, &B.h_exp_cap, 2 * B.tasks.size() * sizeof(double));
+    if (rc) return rc;
+    rc = enqueue_expect(L, B.tasks, prec, B.h_exp);
+    if (rc) return rc;
+  }
+  size_t bit_total = 0;
+  for (ServeReq* r : reqs) bit_total += (size_t)r->shots * r->prog->n;
+  if (bit_total) {
+    rc = grow_pinned((void**)&B.h_bits, &B.h_bits_cap, bit_total);
+    if (rc) return rc;
+    size_t off = 0;
+    for (ServeReq* r : reqs) {
+      if (r->shots <= 0) continue;
+      rc = enqueue_sample(L, r->prog, r->shots, r->seed, B.h_bits + off);
+      if (rc) return rc;
+      B.bit_dst.push_back({r, B.h_bits + off});
+      off += (size_t)r->shots * r->prog->n;
+    }
+  }
+  cudaError_t e = cudaEventRecord(B.ev, L.stream);
+  if (e != cudaSuccess) return fail(MPS_ERR_CUDA, cudaGetErrorString(e));
+  return MPS_OK;
+}
+
+static void serve_loop(mps_ctx* c) {
+  cudaSetDevice(c->device);
+  ServeState* S = c->serve;
+  for (;;) {
+    bool any_busy = false;
+    for (int l = 0; l < kServeLanes; ++l) {
+      if (!S->lane_busy[l]) continue;
+      const cudaError_t e = cudaEventQuery(S->batches[l].ev);
+      if (e == cudaErrorNotReady) {
+        any_busy = true;
+        continue;
+      }
+      finish_batch(S, S->batches[l]);
+      S->lane_busy[l] = 0;
+    }
+    int free_lane = -1;
+    for (int l = 0; l < kServeLanes; ++l)
+      if (!S->lane_busy[l]) {
+        free_lane = l;
+        break;
+      }
+    std::vector<ServeReq*> take;
+    {
+      std::unique_lock<std::mutex> lk(S->mu);
+      if (S->stop && S->queue.empty() && !any_busy) break;
+      if (free_lane >= 0 && !S->queue.empty()) {
+        const int prec = S->queue.front()->prog->prec;
+        size_t bytes = S->inflight_bytes;
+        while (!S->queue.empty()) {
+          ServeReq* r = S->queue.front();
+          if (r->prog->prec != prec) break;
+          if (S->inflight_reqs + (int)take.size() >= S->max_inflight) break;
+          if (!take.empty() && bytes + r->prog->bytes > c->budget) break;
+          bytes += r->prog->bytes;
+          take.push_back(r);
+          S->queue.pop_front();
+        }
+        S->inflight_bytes = bytes;
+        S->inflight_reqs += (int)take.size();
+      } else if (!any_busy && S->queue.empty()) {
+        S->cv_work.wait_for(lk, std::chrono::milliseconds(5));
+        continue;
+      }
+    }
+    if (!take.empty()) {
+      const int rc = launch_batch(c, S, free_lane, take);
+      if (rc) {
+        std::lock_guard<std::mutex> lk(S->mu);
+        for (ServeReq* r : take) {
+          r->status = rc;
+          r->t_done = now_ms();
+          r->done = true;
+        }
+        for (ServeReq* r : take) S->inflight_bytes -= r->prog->bytes;
+        S->inflight_reqs -= (int)take.size();
+        S->batches[free_lane].reqs.clear();
+        S->cv_done.notify_all();
+      } else {
+        S->lane_busy[free_lane] = 1;
+      }
+      continue;
+    }
+    std::this_thread::sleep_for(std::chrono::microseconds(50));
+  }
+}
+
+}  // namespace gbmps
+
+using namespace gbmps;
+
+extern "C" {
+
+int mps_serve_start(mps_ctx* c, int max_inflight) {
+  if (!c) return fail(MPS_ERR_ARG, "ctx is NULL");
+  if (c->serve) return MPS_OK;
+  cudaError_t e = cudaSetDevice(c->device);
+  if (e != cudaSuccess) return fail(MPS_ERR_CUDA, cudaGetErrorString(e));
+  ServeState* S = new ServeState();
+  S->max_inflight = max_inflight > 0 ? max_inflight : 256;
+  S->lanes.resize(kServeLanes);
+  S->batches.resize(kServeLanes);
+  S->lane_busy.assign(kServeLanes, 0);
+  for (int l = 0; l < kServeLanes; ++l) {
+    int rc = lane_init(S->lanes[l]);
+    if (rc) return rc;
+    e = cudaEventCreateWithFlags(&S->batches[l].ev, cudaEventDisableTiming);
+    if (e != cudaSuccess) return fail(MPS_ERR_CUDA, cudaGetErrorString(e));
+    S->batches[l].lane = l;
+  }
+  S->running = true;
+  c->serve = S;
+  S->worker = std::thread(serve_loop, c);
+  return MPS_OK;
+}
+
+int mps_serve_submit(mps_ctx* c, mps_prog* p, int shots, uint64_t seed, uint64_t* ticket) {
+  if (!c || !p || !ticket || shots < 0) return fail(MPS_ERR_ARG, "bad argument");
+  if (!c->serve) return fail(MPS_ERR_STATE, "serve loop not started");
+  if (p->ctx != c) return fail(MPS_ERR_ARG, "program from another context");
+  ServeState* S = c->serve;
+  ServeReq* r = new ServeReq();
+  r->prog = p;
+  r->shots = shots;
+  r->seed = seed;
+  r->t_submit = now_ms();
+  r->t_done = 0.0;
+  r->status = MPS_OK;
+  r->energy = 0.0;
+  r->done = false;
+  int nm = p->measured.empty() ? p->n : (int)p->measured.size();
+  r->bits.assign((size_t)shots * nm, 0);
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    if (S->stop) {
+      delete r;
+      return fail(MPS_ERR_STATE, "serve loop stopping");
+    }
+    r->ticket = S->next_ticket++;
+    S->all[r->ticket] = r;
+    S->queue.push_back(r);
+  }
+  S->cv_work.notify_one();
+  *ticket = r->ticket;
+  return MPS_OK;
+}
+
+int mps_serve_poll(mps_ctx* c, uint64_t ticket, int timeout_ms, double* energy, uint8_t* bits, double* latency_ms) {
+  if (!c) return fail(MPS_ERR_ARG, "ctx is NULL");
+  if (!c->serve) return fail(MPS_ERR_STATE, "serve loop not started");
+  ServeState* S = c->serve;
+  std::unique_lock<std::mutex> lk(S->mu);
+  auto it = S->all.find(ticket);
+  if (it == S->all.end()) return fail(MPS_ERR_ARG, "unknown ticket");
+  ServeReq* r = it->second;
+  const auto pred = [&] { return r->done; };
+  if (timeout_ms < 0)
+    S->cv_done.wait(lk, pred);
+  else if (!S->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), pred))
+    return fail(MPS_ERR_TIMEOUT, "request not finished");
+  const int status = r->status;
+  if (energy) *energy = r->energy;
+  if (bits && !r->bits.empty()) std::memcpy(bits, r->bits.data(), r->bits.size());
+  if (latency_ms) *latency_ms = r->t_done - r->t_submit;
+  S->all.erase(it);
+  delete r;
+  return status;
+}
+
+int mps_serve_stop(mps_ctx* c) {
+  if (!c || !c->serve) return MPS_OK;
+  ServeState* S = c->serve;
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->stop = true;
+  }
+  S->cv_work.notify_all();
+  if (S->worker.joinable()) S->worker.join();
+  cudaSetDevice(c->device);
+  for (int l = 0; l < kServeLanes; ++l) {
+    lane_free(S->lanes[l]);
+    if (S->batches[l].ev) cudaEventDestroy(S->batches[l].ev);
+    if (S->batches[l].h_exp) cudaFreeHost(S->batches[l].h_exp);
+    if (S->batches[l].h_bits) cudaFreeHost(S->batches[l].h_bits);
+  }
+  for (auto& kv : S->all) delete kv.second;
+  delete S;
+  c->serve = nullptr;
+  return MPS_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,376 @@
+"""ctypes binding of the gb300mps C ABI (``include/gb300mps.h``).
+
+This is the Python face of the engine: a ``Context`` owns the GPU stream and
+memory, a ``Program`` is one MPS register with the gates recorded on it.  The
+library must have been built (``tnqvm_gb300.build``); there is no CPU path and
+loading fails loudly when the shared object is missing.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libgb300mps.so")
+
+OK, ERR_ARG, ERR_OOM, ERR_TIMEOUT, ERR_NUMERIC, ERR_CUDA, ERR_STATE, ERR_UNSUPPORTED = range(8)
+TRUNC_EXATN, TRUNC_ITENSOR = 0, 1
+PREC_FP64, PREC_FP32 = 0, 1
+FLAG_RENORM, FLAG_PER_GATE = 1, 2
+CHI_LIMIT = 64
+
+_ERR_NAMES = {1: "MPS_ERR_ARG", 2: "MPS_ERR_OOM", 3: "MPS_ERR_TIMEOUT", 4: "MPS_ERR_NUMERIC",
+              5: "MPS_ERR_CUDA", 6: "MPS_ERR_STATE", 7: "MPS_ERR_UNSUPPORTED"}
+
+# (name, restype, argtypes) for every exported function
+_c = ctypes
+_P = _c.c_void_p
+_DP = _c.POINTER(_c.c_double)
+SIGNATURES = [
+    ("mps_last_error", _c.c_char_p, []),
+    ("mps_version", _c.c_char_p, []),
+    ("mps_ctx_create", _c.c_int, [_P, _c.POINTER(_P)]),
+    ("mps_ctx_destroy", _c.c_int, [_P]),
+    ("mps_ctx_info", _c.c_int, [_P, _c.POINTER(_c.c_int), _c.POINTER(_c.c_size_t)]),
+    ("mps_program_begin", _c.c_int, [_P, _c.c_int, _c.c_int, _c.c_double, _c.c_int, _c.c_int, _c.c_int,
+                                      _c.POINTER(_P)]),
+    ("mps_program_reset", _c.c_int, [_P]),
+    ("mps_program_destroy", _c.c_int, [_P]),
+    ("mps_gate1", _c.c_int, [_P, _c.c_int, _DP]),
+    ("mps_gate2", _c.c_int, [_P, _c.c_int, _c.c_int, _DP]),
+    ("mps_gate_named", _c.c_int, [_P, _c.c_char_p, _c.POINTER(_c.c_int), _c.c_int, _DP, _c.c_int]),
+    ("mps_measure", _c.c_int, [_P, _c.c_int]),
+    ("mps_submit", _c.c_int, [_P]),
+    ("mps_wait", _c.c_int, [_P, _c.c_int]),
+    ("mps_batch_submit", _c.c_int, [_P, _c.POINTER(_P), _c.c_int]),
+    ("mps_norm", _c.c_int, [_P, _DP]),
+    ("mps_amplitudes", _c.c_int, [_P, _DP]),
+    ("mps_amplitude", _c.c_int, [_P, _c.POINTER(_c.c_int), _DP]),
+    ("mps_expect_pauli", _c.c_int, [_P, _c.c_char_p, _c.c_int, _DP, _DP]),
+    ("mps_set_observable", _c.c_int, [_P, _c.c_char_p, _c.c_int, _DP]),
+    ("mps_batch_expect", _c.c_int, [_P, _c.POINTER(_P), _c.c_int, _DP]),
+    ("mps_sample", _c.c_int, [_P, _c.c_int, _c.c_uint64, _c.POINTER(_c.c_uint8)]),
+    ("mps_n_measured", _c.c_int, [_P, _c.POINTER(_c.c_int)]),
+    ("mps_truncation_fidelity", _c.c_int, [_P, _DP]),
+    ("mps_bond_dims", _c.c_int, [_P, _c.POINTER(_c.c_int)]),
+    ("mps_stats", _c.c_int, [_P, _DP]),
+    ("mps_serve_start", _c.c_int, [_P, _c.c_int]),
+    ("mps_serve_submit", _c.c_int, [_P, _P, _c.c_int, _c.c_uint64, _c.POINTER(_c.c_uint64)]),
+    ("mps_serve_poll", _c.c_int, [_P, _c.c_uint64, _c.c_int, _DP, _c.POINTER(_c.c_uint8), _DP]),
+    ("mps_serve_stop", _c.c_int, [_P]),
+    ("mps_footprint_bytes", _c.c_size_t, [_c.c_int, _c.c_int, _c.c_int]),
+    ("mps_graph_create", _c.c_int, [_P, _c.POINTER(_P), _c.c_int, _c.POINTER(_P)]),
+    ("mps_graph_launch", _c.c_int, [_P, _DP]),
+    ("mps_graph_launch_async", _c.c_int, [_P]),
+    ("mps_graph_sync", _c.c_int, [_P, _DP]),
+    ("mps_graph_update", _c.c_int, [_P]),
+    ("mps_graph_stream", _c.c_int, [_P, _c.POINTER(_P)]),
+    ("mps_graph_destroy", _c.c_int, [_P]),
+    ("mps_graph_timing", _c.c_int, [_P, _DP]),
+    ("mps_gates", _c.c_int, [_P, _c.c_int, _c.POINTER(_c.c_int32), _c.POINTER(_c.c_int32), _DP]),
+]
+
+GATE_IDS = {name: i for i, name in enumerate(
+    ["I", "H", "CNOT", "Rx", "Ry", "Rz", "Swap", "U", "X", "Y", "Z", "Measure", "CZ", "CPhase", "S", "Sdg",
+     "T", "Tdg", "CY", "CH", "CRZ", "iSwap", "fSim", "RZZ"])}
+GATE_IDS["CX"] = GATE_IDS["CNOT"]
+GATE_IDS["U3"] = GATE_IDS["U"]
+
+
+def encode_circuit(circuit):
+    """Gate list -> (ids int32[g], qubits int32[g,2], params float64[g,3]) for ``Program.record``."""
+    g = len(circuit)
+    ids = np.zeros(g, dtype=np.int32)
+    qs = np.zeros((g, 2), dtype=np.int32)
+    ps = np.zeros((g, 3), dtype=np.float64)
+    for i, (name, q, p) in enumerate(circuit):
+        ids[i] = GATE_IDS[name]
+        qs[i, : len(q)] = q
+        ps[i, : len(p)] = p
+    return ids, qs, ps
+
+_lib = None
+
+
+class MpsError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s: %s" % (_ERR_NAMES.get(code, str(code)), msg))
+        self.code = code
+
+
+def load_library(path=LIB_PATH):
+    """Load the engine.  Raises if the CUDA library was not built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise ImportError("libgb300mps.so not built (run tnqvm_gb300.build.build()); "
+                          "there is no CPU fallback")
+    lib = ctypes.CDLL(path)
+    for name, res, args in SIGNATURES:
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _check(rc):
+    if rc != OK:
+        raise MpsError(rc, _lib.mps_last_error().decode())
+
+
+def _dptr(a):
+    return a.ctypes.data_as(_DP)
+
+
+class _Cfg(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int), ("hbm_budget_bytes", ctypes.c_size_t)]
+
+
+class Context:
+    def __init__(self, device=0, hbm_budget_bytes=0):
+        lib = load_library()
+        cfg = _Cfg(device, hbm_budget_bytes)
+        h = ctypes.c_void_p()
+        _check(lib.mps_ctx_create(ctypes.byref(cfg), ctypes.byref(h)))
+        self.h = h
+        self.serving = False
+
+    def close(self):
+        if self.h:
+            _lib.mps_ctx_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def num_sms(self):
+        n = ctypes.c_int()
+        _check(_lib.mps_ctx_info(self.h, ctypes.byref(n), None))
+        return n.value
+
+    @property
+    def bytes_resident(self):
+        b = ctypes.c_size_t()
+        _check(_lib.mps_ctx_info(self.h, None, ctypes.byref(b)))
+        return b.value
+
+    # ---- batches
+    def batch_submit(self, programs):
+        arr = (ctypes.c_void_p * len(programs))(*[p.h for p in programs])
+        _check(_lib.mps_batch_submit(self.h, arr, len(programs)))
+
+    def batch_expect(self, programs):
+        arr = (ctypes.c_void_p * len(programs))(*[p.h for p in programs])
+        out = np.zeros(len(programs))
+        _check(_lib.mps_batch_expect(self.h, arr, len(programs), _dptr(out)))
+        return out
+
+    # ---- serving
+    def serve_start(self, max_inflight=256):
+        _check(_lib.mps_serve_start(self.h, max_inflight))
+        self.serving = True
+
+    def serve_submit(self, program, shots=0, seed=0):
+        t = ctypes.c_uint64()
+        _check(_lib.mps_serve_submit(self.h, program.h, shots, seed, ctypes.byref(t)))
+        return t.value
+
+    def serve_poll(self, ticket, program, shots=0, timeout_ms=-1):
+        """Returns (energy, bits[shots, n_meas], latency_ms)."""
+        e = ctypes.c_double()
+        lat = ctypes.c_double()
+        nm = program.n_measured
+        bits = np.zeros((max(shots, 0), nm), dtype=np.uint8)
+        bp = bits.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)) if shots > 0 else None
+        _check(_lib.mps_serve_poll(self.h, ticket, timeout_ms, ctypes.byref(e), bp, ctypes.byref(lat)))
+        return e.value, bits, lat.value
+
+    def serve_stop(self):
+        _check(_lib.mps_serve_stop(self.h))
+        self.serving = False
+
+
+class Graph:
+    """Captured batch: reset + one persistent launch + observables + D2H,
+    replayed by ``launch``; ``update`` loads newly recorded gates of the same
+    structure (new parameters) into the captured op table."""
+
+    def __init__(self, ctx, programs):
+        self.programs = list(programs)
+        arr = (ctypes.c_void_p * len(programs))(*[p.h for p in programs])
+        h = ctypes.c_void_p()
+        _check(_lib.mps_graph_create(ctx.h, arr, len(programs), ctypes.byref(h)))
+        self.h = h
+        self.out = np.zeros(len(programs))
+
+    def launch(self):
+        _check(_lib.mps_graph_launch(self.h, _dptr(self.out)))
+        return self.out.copy()
+
+    def launch_async(self):
+        _check(_lib.mps_graph_launch_async(self.h))
+
+    def sync(self):
+        _check(_lib.mps_graph_sync(self.h, _dptr(self.out)))
+        return self.out.copy()
+
+    def update(self):
+        _check(_lib.mps_graph_update(self.h))
+
+    def timing(self):
+        """(ms reset+ops, ms observables, GEMM-class flops, eigensolver flops) of the last replay."""
+        out = np.zeros(4)
+        _check(_lib.mps_graph_timing(self.h, _dptr(out)))
+        return tuple(out)
+
+    @property
+    def stream(self):
+        s = ctypes.c_void_p()
+        _check(_lib.mps_graph_stream(self.h, ctypes.byref(s)))
+        return s.value
+
+    def close(self):
+        if self.h:
+            _lib.mps_graph_destroy(self.h)
+            self.h = None
+
+
+def footprint_bytes(n, chi_max, precision):
+    load_library()
+    return _lib.mps_footprint_bytes(n, chi_max, precision)
+
+
+class Program:
+    """One MPS register.  ``mode``: TRUNC_EXATN or TRUNC_ITENSOR;
+    ``precision``: PREC_FP64 or PREC_FP32; ``chi_max <= 0`` means the build's
+    limit; ``cutoff < 0`` selects the visitor default."""
+
+    def __init__(self, ctx, n, chi_max=0, cutoff=-1.0, mode=TRUNC_EXATN, precision=PREC_FP64, flags=0):
+        self.ctx = ctx
+        self.n = n
+        h = ctypes.c_void_p()
+        _check(_lib.mps_program_begin(ctx.h, n, chi_max, cutoff, mode, precision, flags, ctypes.byref(h)))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            _lib.mps_program_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def reset(self):
+        _check(_lib.mps_program_reset(self.h))
+
+    # ---- gates
+    def gate(self, name, qubits, params=()):
+        q = (ctypes.c_int * len(qubits))(*qubits)
+        p = np.ascontiguousarray(params, dtype=np.float64)
+        _check(_lib.mps_gate_named(self.h, name.encode(), q, len(qubits), _dptr(p) if p.size else None, p.size))
+
+    def gate1(self, q, m):
+        a = np.ascontiguousarray(np.asarray(m, dtype=np.complex128).reshape(2, 2)).view(np.float64).reshape(-1)
+        _check(_lib.mps_gate1(self.h, q, _dptr(a)))
+
+    def gate2(self, q0, q1, m):
+        a = np.ascontiguousarray(np.asarray(m, dtype=np.complex128).reshape(4, 4)).view(np.float64).reshape(-1)
+        _check(_lib.mps_gate2(self.h, q0, q1, _dptr(a)))
+
+    def measure(self, q):
+        _check(_lib.mps_measure(self.h, q))
+
+    def run(self, circuit):
+        """Record ``[(name, qubits, params), ...]`` (Measure included)."""
+        for name, qs, ps in circuit:
+            self.gate(name, list(qs), list(ps))
+        return self
+
+    def record(self, encoded):
+        """Bulk-record an ``encode_circuit`` result with one C call."""
+        ids, qs, ps = encoded
+        _check(_lib.mps_gates(self.h, len(ids), ids.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                              qs.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), _dptr(ps)))
+        return self
+
+    def submit(self):
+        _check(_lib.mps_submit(self.h))
+
+    def wait(self, timeout_ms=-1):
+        _check(_lib.mps_wait(self.h, timeout_ms))
+
+    # ---- results
+    def norm(self):
+        v = ctypes.c_double()
+        _check(_lib.mps_norm(self.h, ctypes.byref(v)))
+        return v.value
+
+    def amplitudes(self):
+        out = np.zeros(2 << self.n, dtype=np.float64)
+        _check(_lib.mps_amplitudes(self.h, _dptr(out)))
+        return out.view(np.complex128)
+
+    def amplitude(self, bits):
+        b = (ctypes.c_int * self.n)(*bits)
+        out = np.zeros(2)
+        _check(_lib.mps_amplitude(self.h, b, _dptr(out)))
+        return complex(out[0], out[1])
+
+    def expect_pauli(self, paulis, coeffs=None):
+        """Returns complex <P_t> per term (unnormalised) and, with coeffs,
+        also sum_t c_t Re<P_t>."""
+        paulis = list(paulis)
+        for s in paulis:
+            if len(s) != self.n:
+                raise ValueError("Pauli string length must equal the qubit count")
+        buf = "".join(paulis).encode()
+        out = np.zeros(2 * len(paulis) + 1)
+        c = None
+        if coeffs is not None:
+            c = np.ascontiguousarray(coeffs, dtype=np.float64)
+        _check(_lib.mps_expect_pauli(self.h, buf, len(paulis), _dptr(c) if c is not None else None, _dptr(out)))
+        vals = out[: 2 * len(paulis)].view(np.complex128).copy()
+        if coeffs is not None:
+            return vals, float(out[2 * len(paulis)])
+        return vals
+
+    def set_observable(self, paulis, coeffs):
+        paulis = list(paulis)
+        c = np.ascontiguousarray(coeffs, dtype=np.float64)
+        _check(_lib.mps_set_observable(self.h, "".join(paulis).encode(), len(paulis), _dptr(c)))
+
+    @property
+    def n_measured(self):
+        v = ctypes.c_int()
+        _check(_lib.mps_n_measured(self.h, ctypes.byref(v)))
+        return v.value
+
+    def sample(self, shots, seed=0):
+        nm = self.n_measured
+        out = np.zeros((shots, nm), dtype=np.uint8)
+        _check(_lib.mps_sample(self.h, shots, seed, out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))))
+        return out
+
+    def truncation_fidelity(self):
+        v = ctypes.c_double()
+        _check(_lib.mps_truncation_fidelity(self.h, ctypes.byref(v)))
+        return v.value
+
+    def bond_dims(self):
+        out = (ctypes.c_int * max(self.n - 1, 1))()
+        _check(_lib.mps_bond_dims(self.h, out))
+        return list(out)[: self.n - 1]
+
+    def stats(self):
+        out = np.zeros(4)
+        _check(_lib.mps_stats(self.h, _dptr(out)))
+        return {"fidelity": out[0], "max_discarded": out[1], "gate2": int(out[2]), "ops": int(out[3])}

@@ -1,0 +1,221 @@
+"""Python mirror of TNQVM's visitor plugin interface for the GB300 MPS engine.
+
+``GpuMpsVisitor`` has the method set of ``tnqvm::TNQVMVisitor``
+(``tnqvm/visitors/TNQVMVisitor.hpp:58-82``): ``initialize(buffer, shots)``,
+one ``visit`` per gate, ``finalize()``, ``getExpectationValueZ(circuit)``,
+``getState()``, ``supportVqeMode()``, ``name()``.  Results go to an
+``AcceleratorBuffer`` stand-in with XACC's ``addExtraInfo`` /
+``appendMeasurement`` keys (``exp-val-z``, ``norm``, ``amplitude-real``,
+``amplitude-imag``, ``amplitude-real-vec``, ``amplitude-imag-vec``).  The C++
+plugin (``tnqvm_gb300/visitor/``) is the same logic against the XACC headers.
+
+Options (``setOptions``), as in ``TNQVM::updateConfiguration``
+(``tnqvm/TNQVM.hpp:61-125``) and the exatn-mps visitor
+(``ExaTnMpsVisitor.cpp:257-271``): ``svd-cutoff`` (default DBL_MIN),
+``max-bond-dim`` (default: the build's limit), ``shots``, ``seed``, plus
+``truncation-mode`` (``exatn`` | ``itensor``), ``precision`` (``fp64`` |
+``fp32``), ``renormalize`` and ``per-gate`` (one launch per gate).
+"""
+from collections import Counter
+
+import numpy as np
+
+from . import mps as M
+
+MAX_NUMBER_QUBITS_FOR_STATE_VEC = 20   # ExaTnMpsVisitor.cpp:55
+
+
+class AcceleratorBuffer:
+    """Result sink with the XACC AcceleratorBuffer calls the visitors use."""
+
+    def __init__(self, n):
+        self.n = n
+        self.extra = {}
+        self.counts = Counter()
+
+    def size(self):
+        return self.n
+
+    def addExtraInfo(self, key, value):
+        self.extra[key] = value
+
+    def __getitem__(self, key):
+        return self.extra[key]
+
+    def __contains__(self, key):
+        return key in self.extra
+
+    def appendMeasurement(self, bits, count=1):
+        self.counts[bits] += count
+
+    def getMeasurementCounts(self):
+        return dict(self.counts)
+
+    def computeMeasurementProbability(self, bits):
+        tot = sum(self.counts.values())
+        return self.counts.get(bits, 0) / tot if tot else 0.0
+
+    def getExpectationValueZ(self):
+        if "exp-val-z" in self.extra:
+            return self.extra["exp-val-z"]
+        tot = sum(self.counts.values())
+        if tot == 0:
+            return 0.0
+        e = 0.0
+        for k, v in self.counts.items():
+            e += (-1.0 if k.count("1") % 2 else 1.0) * v
+        return e / tot
+
+
+_CTX = None
+
+
+def default_context():
+    global _CTX
+    if _CTX is None:
+        _CTX = M.Context(0)
+    return _CTX
+
+
+class GpuMpsVisitor:
+    """``tnqvm-visitor`` name ``gb300-mps``."""
+
+    def __init__(self, ctx=None):
+        self.ctx = ctx
+        self.options = {}
+        self.prog = None
+        self.buffer = None
+        self.shots = 1
+        self.execution_info = {}
+
+    # ---- plugin identity (Identifiable / Cloneable)
+    def name(self):
+        return "gb300-mps"
+
+    def description(self):
+        return "Matrix-product-state simulator on one GB300 GPU (sm_103a kernels)"
+
+    def clone(self):
+        v = GpuMpsVisitor(self.ctx)
+        v.options = dict(self.options)
+        return v
+
+    def supportVqeMode(self):
+        return True
+
+    def setOptions(self, options):
+        self.options = dict(options)
+
+    def getExecutionInfo(self):
+        return dict(self.execution_info)
+
+    # ---- lifecycle
+    def initialize(self, buffer, nbShots=1):
+        if self.ctx is None:
+            self.ctx = default_context()
+        o = self.options
+        mode = {"exatn": M.TRUNC_EXATN, "itensor": M.TRUNC_ITENSOR}[o.get("truncation-mode", "exatn")]
+        prec = {"fp64": M.PREC_FP64, "fp32": M.PREC_FP32}[o.get("precision", "fp64")]
+        flags = (M.FLAG_RENORM if o.get("renormalize", False) else 0) | \
+                (M.FLAG_PER_GATE if o.get("per-gate", False) else 0)
+        cutoff = float(o["svd-cutoff"]) if "svd-cutoff" in o else -1.0
+        chi = int(o["max-bond-dim"]) if "max-bond-dim" in o else 0
+        if self.prog is not None:
+            self.prog.close()
+        self.buffer = buffer
+        self.shots = nbShots
+        self.prog = M.Program(self.ctx, buffer.size(), chi, cutoff, mode, prec, flags)
+        self.measured = []
+
+    def visit(self, name, qubits, params=()):
+        if name == "Measure":
+            self.measured.append(qubits[0])
+            self.prog.measure(qubits[0])
+            return
+        self.prog.gate(name, list(qubits), list(params))
+
+    def run(self, circuit):
+        for name, qs, ps in circuit:
+            self.visit(name, qs, ps)
+
+    def finalize(self):
+        """ExaTnMpsVisitor::finalize (ExaTnMpsVisitor.cpp:576-681)."""
+        p, buf = self.prog, self.buffer
+        n = buf.size()
+        p.submit()
+        p.wait()
+        st = p.stats()
+        self.execution_info.update({"truncation-fidelity": st["fidelity"],
+                                    "max-discarded-weight": st["max_discarded"]})
+        bitstring = self.options.get("bitstring")
+        if bitstring is not None:
+            self._bitstring(bitstring)
+            return
+        if n < MAX_NUMBER_QUBITS_FOR_STATE_VEC:
+            buf.addExtraInfo("norm", p.norm())
+            if self.measured:
+                if self.shots < 1:
+                    z = "".join("Z" if (self.measured.count(q) % 2) else "I" for q in range(n))
+                    buf.addExtraInfo("exp-val-z", float(p.expect_pauli([z])[0].real))
+                else:
+                    self._sample(self.shots)
+        elif self.measured:
+            self._sample(max(self.shots, 1))
+
+    def _sample(self, shots):
+        seed = int(self.options.get("seed", np.random.SeedSequence().entropy % (1 << 63)))
+        bits = self.prog.sample(shots, seed)
+        keys = ["".join(map(str, row)) for row in bits]
+        for k, v in Counter(keys).items():
+            self.buffer.appendMeasurement(k, v)
+
+    def _bitstring(self, bits):
+        """``bitstring`` option (ExaTnMpsVisitor.cpp:776-822): -1 marks an open
+        qubit; one amplitude, or the normalised slice over the open qubits."""
+        n = self.buffer.size()
+        if len(bits) != n:
+            raise ValueError("Bitstring size must match the number of qubits.")
+        open_q = [i for i, b in enumerate(bits) if b == -1]
+        if not open_q:
+            a = self.prog.amplitude([int(b) for b in bits])
+            self.buffer.addExtraInfo("amplitude-real", a.real)
+            self.buffer.addExtraInfo("amplitude-imag", a.imag)
+            return
+        vals = []
+        for k in range(1 << len(open_q)):
+            b = list(bits)
+            for j, q in enumerate(open_q):
+                b[q] = (k >> j) & 1
+            vals.append(self.prog.amplitude(b))
+        v = np.array(vals)
+        nrm = float(np.sum(np.abs(v) ** 2))
+        if nrm > 1e-12:
+            v = v / np.sqrt(nrm)
+        self.buffer.addExtraInfo("amplitude-real-vec", list(v.real))
+        self.buffer.addExtraInfo("amplitude-imag-vec", list(v.imag))
+
+    def getState(self):
+        return self.prog.amplitudes()
+
+    def getExpectationValueZ(self, observed_circuit):
+        """VQE mode: ``observed_circuit`` is the basis change plus Measure gates
+        of one Pauli term (``TNQVM.cpp:82-89``).  The basis change is folded
+        into a local Pauli on the resident MPS instead of re-simulating
+        (X basis: H, Y basis: Rx(pi/2), as XACC's observed composites emit)."""
+        n = self.buffer.size()
+        letters = ["I"] * n
+        pending = {}
+        for name, qs, ps in observed_circuit:
+            if name == "Measure":
+                q = qs[0]
+                letters[q] = pending.get(q, "Z")
+            elif name == "H":
+                pending[qs[0]] = "X"
+            elif name == "Rx" and abs(abs(ps[0]) - np.pi / 2) < 1e-12:
+                pending[qs[0]] = "Y"
+            else:
+                raise ValueError("unsupported basis-change gate %s" % name)
+        if all(c == "I" for c in letters):
+            return 0.0
+        v = self.prog.expect_pauli(["".join(letters)])[0]
+        return float(v.real)
