@@ -346,3 +346,19 @@ def test_vqe_mode_observed_circuits(ctx):
            ("Measure", (2,), ())]
     e = v.getExpectationValueZ(obs)
     assert abs(e - dense.expect_pauli(psi, n, "XZYI").real) < TOL64
+
+
+def test_engine_matches_itensor_reference_fixtures(ctx):
+    """complex128 engine in itensor semantics vs the reference's vendored
+    ITensor v3 outputs (tests/golden/itensor_fixtures.json): same bond
+    dimensions, <P> within 1e-10."""
+    import json
+    import os
+    fx = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "itensor_fixtures.json")))
+    for c in fx["cases"]:
+        circ = [(g, tuple(q), tuple(p)) for g, q, p in c["circuit"]]
+        with run(ctx, c["n"], circ, c["chi"], c["cutoff"], M.TRUNC_ITENSOR, M.PREC_FP64) as p:
+            assert p.bond_dims() == c["bonds"], c["name"]
+            vals = p.expect_pauli(c["paulis"])
+            for s, v, want in zip(c["paulis"], vals, c["expect"]):
+                assert abs(v - complex(*want)) < TOL64, (c["name"], s)

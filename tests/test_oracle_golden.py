@@ -241,3 +241,21 @@ def test_truncated_modes_consistent():
     m = mps.run(n, circ, mode="itensor", chi_max=4, cutoff=1e-12)
     assert max(m.bond_dims()) <= 4
     assert abs(m.norm2() - m.fidelity) < 1e-10   # canonical truncation: norm^2 = prod(1 - eps)
+
+
+def test_oracle_matches_itensor_reference_fixtures():
+    """itensor-mode oracle vs the reference's vendored ITensor v3 run on the
+    same routed circuits (tests/golden/itensor_fixtures.json, produced by
+    tests/golden/make_itensor_fixtures.py): identical bond dimensions under
+    cap and relative-cutoff truncation, <P> to 1e-12."""
+    import json
+    import os
+    path = os.path.join(os.path.dirname(__file__), "golden", "itensor_fixtures.json")
+    fx = json.load(open(path))
+    assert len(fx["cases"]) >= 6
+    for c in fx["cases"]:
+        circ = [(g, tuple(q), tuple(p)) for g, q, p in c["circuit"]]
+        m = mps.run(c["n"], circ, mode="itensor", chi_max=c["chi"], cutoff=c["cutoff"])
+        assert m.bond_dims() == c["bonds"], c["name"]
+        for p, v in zip(c["paulis"], c["expect"]):
+            assert abs(m.expect_pauli(p) - complex(*v)) < 1e-12, (c["name"], p)

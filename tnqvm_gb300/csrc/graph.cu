@@ -163,15 +163,15 @@ int mps_graph_create(mps_ctx* c, mps_prog* const* progs, int n, mps_graph** out)
   for (int i = 0; i < 3; ++i)
     if (cudaEventCreate(&g->ev[i]) != cudaSuccess) return bail(fail(MPS_ERR_CUDA, "event creation failed"));
   GCK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-  cudaError_t e = cudaEventRecord(g->ev[0], st);
+  cudaError_t e = cudaEventRecordWithFlags(g->ev[0], st, cudaEventRecordExternal);
   if (e == cudaSuccess) e = launch_reset(prec, L.d_desc, n, st);
   if (e == cudaSuccess) e = cudaMemsetAsync(L.d_queue, 0, sizeof(int), st);
   if (e == cudaSuccess) e = launch_ops(prec, L.d_desc, n, grid, n > 1 ? L.d_queue : nullptr, L.op_scratch[prec], st);
-  if (e == cudaSuccess) e = cudaEventRecord(g->ev[1], st);
+  if (e == cudaSuccess) e = cudaEventRecordWithFlags(g->ev[1], st, cudaEventRecordExternal);
   if (e == cudaSuccess && nt > 0) e = launch_expect(prec, L.d_exp_tasks, nt, L.exp_scratch[prec], L.d_exp_out, st);
   if (e == cudaSuccess && nt > 0)
     e = cudaMemcpyAsync(g->h_out, L.d_exp_out, 2 * (size_t)nt * sizeof(double), cudaMemcpyDeviceToHost, st);
-  if (e == cudaSuccess) e = cudaEventRecord(g->ev[2], st);
+  if (e == cudaSuccess) e = cudaEventRecordWithFlags(g->ev[2], st, cudaEventRecordExternal);
   cudaGraph_t graph = nullptr;
   const cudaError_t e2 = cudaStreamEndCapture(st, &graph);
   if (e != cudaSuccess || e2 != cudaSuccess) {
@@ -230,7 +230,7 @@ int mps_graph_launch(mps_graph* g, double* energies) {
   return mps_graph_sync(g, energies);
 }
 
-int mps_graph_timing(mps_graph* g, double out[4]) {
+int mps_graph_timing(mps_graph* g, double out[6]) {
   if (!g || !out) return fail(MPS_ERR_ARG, "NULL argument");
   GCK(cudaSetDevice(g->c->device));
   GCK(cudaStreamSynchronize(g->L.stream));
@@ -248,6 +248,8 @@ int mps_graph_timing(mps_graph* g, double out[4]) {
   }
   out[2] = fl;
   out[3] = ef;
+  out[4] = (double)(g->flat.size() * sizeof(DevOp));
+  out[5] = (double)(2 * g->tasks.size() * sizeof(double));
   return MPS_OK;
 }
 

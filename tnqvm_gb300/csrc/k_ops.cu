@@ -118,7 +118,10 @@ __device__ int jacobi_eigh(cx<T>* Gp, cx<T>* U, int m, double trace, SmallSmem<T
   __syncthreads();
   const int np = m >> 1;
   const T tol_rel = T(Prec<T>::eps);
-  const T tol_abs = T(Prec<T>::eps * trace);
+  // Relative threshold only, with a floor far below FP rounding of the trace: an
+  // absolute eps*trace floor leaves off-diagonals that mix kept and discarded
+  // eigenvectors across small gaps and costs accuracy after truncation.
+  const T tol_abs = T(64.0 * Prec<T>::eps * Prec<T>::eps * trace);
   for (int sweep = 0; sweep < Prec<T>::max_sweeps; ++sweep) {
     if (tid == 0) sm->ival[0] = 0;
     __syncthreads();
@@ -467,7 +470,8 @@ __device__ void op_gate2(const ProgDesc& P, const DevOp& op, char* big, SmallSme
     if (frac > P.stats[ST_MAX_DISC]) P.stats[ST_MAX_DISC] = frac;
     P.stats[ST_N_GATE2] += 1.0;
     // algorithmic flops (complex MAC = 8): merge, gate, Gram, split
-    P.stats[ST_FLOPS] += 32.0 * dl * dm * dr + 128.0 * dl * dr + 8.0 * m * m * nn + 8.0 * k * nn * m;
+    P.stats[ST_FLOPS] += 32.0 * dl * dm * dr + 128.0 * dl * dr + 8.0 * m * m * nn + 8.0 * k * nn * m +
+                         (Prec<T>::u_in_smem ? 16.0 * m * k * k : 0.0);
     // each rotation updates two rows and two columns of G and two columns of U
     P.stats[ST_EIG_FLOPS] += 96.0 * m * nrot_total;
     if (bad) atomicOr(P.err, ERR_NAN);
@@ -488,12 +492,51 @@ __device__ void op_gate2(const ProgDesc& P, const DevOp& op, char* big, SmallSme
     }
   }
   __syncthreads();
+  // Kept eigenvectors W_k (m x k, ld k).  In FP32 the ~m*sweeps accumulated
+  // rotations leave the columns ~1e-5 off orthonormal, which would drift the
+  // norm by that much per gate; one Newton-Schulz step
+  // W <- W - 1/2 W (W^H W - I) restores orthonormality to FP32 rounding.
+  // The Gram region holds the compacted W, the U region E and the result.
+  const cx<T>* W;
+  if (Prec<T>::u_in_smem) {
+    cx<T>* Wc = reinterpret_cast<cx<T>*>(big);
+    for (int t = tid; t < m * k; t += nt) {
+      const int i = t / k, j = t - i * k;
+      Wc[t] = U[i * m + sm->perm[j]];
+    }
+    __syncthreads();
+    cx<T>* E = U;
+    cx<T>* Wn = U + k * k;
+    for (int t = tid; t < k * k; t += nt) {
+      const int a = t / k, b = t - a * k;
+      cx<T> acc = mk<T>(0, 0);
+      for (int i = 0; i < m; ++i) fma_cj(acc, Wc[i * k + a], Wc[i * k + b]);
+      if (a == b) acc.re -= T(1);
+      E[t] = acc;
+    }
+    __syncthreads();
+    for (int t = tid; t < m * k; t += nt) {
+      const int i = t / k, j = t - i * k;
+      cx<T> corr = mk<T>(0, 0);
+      for (int l = 0; l < k; ++l) fma_c(corr, Wc[i * k + l], E[l * k + j]);
+      Wn[t] = Wc[t] - scl(corr, T(0.5));
+    }
+    __syncthreads();
+    W = Wn;
+  } else {
+    cx<T>* Wc = reinterpret_cast<cx<T>*>(big);
+    for (int t = tid; t < m * k; t += nt) {
+      const int i = t / k, j = t - i * k;
+      Wc[t] = U[i * m + sm->perm[j]];
+    }
+    __syncthreads();
+    W = Wc;
+  }
   // other side: Z = W_k^H X (k x nn)
   for (int t = tid; t < k * nn; t += nt) {
     const int j = t / nn, c = t - j * nn;
-    const int pj = sm->perm[j];
     cx<T> acc = mk<T>(0, 0);
-    for (int i = 0; i < m; ++i) fma_cj(acc, U[i * m + pj], X(i, c));
+    for (int i = 0; i < m; ++i) fma_cj(acc, W[i * k + j], X(i, c));
     acc = scl(acc, sm->oth[j]);
     if (!tr)
       B[j * Cc + c] = acc;  // hi site (k, 2, dr)
@@ -503,7 +546,7 @@ __device__ void op_gate2(const ProgDesc& P, const DevOp& op, char* big, SmallSme
   // isometric side: W_k
   for (int t = tid; t < m * k; t += nt) {
     const int i = t / k, j = t - i * k;
-    const cx<T> w = scl(U[i * m + sm->perm[j]], sm->iso[j]);
+    const cx<T> w = scl(W[i * k + j], sm->iso[j]);
     if (!tr)
       A[i * k + j] = w;   // lo site (dl, 2, k)
     else

@@ -224,8 +224,9 @@ class Graph:
         _check(_lib.mps_graph_update(self.h))
 
     def timing(self):
-        """(ms reset+ops, ms observables, GEMM-class flops, eigensolver flops) of the last replay."""
-        out = np.zeros(4)
+        """(ms reset+ops, ms observables, GEMM-class flops, eigensolver flops,
+        op-table bytes per update, result bytes per replay) of the last replay."""
+        out = np.zeros(6)
         _check(_lib.mps_graph_timing(self.h, _dptr(out)))
         return tuple(out)
 
