@@ -186,7 +186,7 @@ def run_ours(args):
     from tnqvm_gb300 import mps as M
 
     ctx = M.Context(local)
-    insts = circuits.vqe_batch(args.instances, seed=2024 + rank)   # replicas: one shard per rank
+    insts = circuits.vqe_batch(args.instances, seed=2024 + rank, qmax=args.qmax, lmax=args.lmax)  # replica shard
     enc = [M.encode_circuit(it["circuit"]) for it in insts]
     progs = []
     for it, e in zip(insts, enc):
@@ -383,6 +383,8 @@ def main():
     ap.add_argument("--ref-sample", type=int, default=4)
     ap.add_argument("--serve-requests", type=int, default=256)
     ap.add_argument("--no-extras", action="store_true")
+    ap.add_argument("--qmax", type=int, default=32, help="largest qubit count (small profiling cases)")
+    ap.add_argument("--lmax", type=int, default=12, help="largest layer count (small profiling cases)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -1,0 +1,57 @@
+"""The C++ TNQVM visitor plugin (GpuMpsVisitor against the XACC interface
+shim): it compiles and links here; on a GPU, circuits driven through it the
+way TNQVM::execute does (TNQVM.cpp:106-139) give the oracle's results."""
+import json
+import subprocess
+
+import numpy as np
+import pytest
+
+from oracle import dense
+from tnqvm_gb300 import build as B
+from tnqvm_gb300 import circuits
+
+
+def test_plugin_compiles_and_links():
+    path = B.build_visitor_demo()
+    assert path.endswith("visitor_demo")
+
+
+def _script(n, shots, circ, opts=()):
+    lines = ["%d %d" % (n, shots)]
+    for k, v in opts:
+        lines.append("opt %s %s" % (k, v))
+    for name, qs, ps in circ:
+        lines.append("%s %d %s %d %s" % (name, len(qs), " ".join(map(str, qs)), len(ps),
+                                         " ".join("%.17g" % p for p in ps)))
+    return "\n".join(lines) + "\n"
+
+
+def _run(n, shots, circ, opts=()):
+    exe = B.build_visitor_demo()
+    r = subprocess.run([exe], input=_script(n, shots, circ, opts), capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    return json.loads(r.stdout)
+
+
+@pytest.mark.gpu
+def test_plugin_exp_val_z_and_norm():
+    n = 10
+    circ = circuits.brickwall(n, 6, seed=4) + [("Measure", (q,), ()) for q in (0, 3, 7)]
+    psi = dense.run(n, circ)
+    out = _run(n, 0, circ, [("max-bond-dim", 32), ("svd-cutoff", 1e-14)])
+    assert out["name"] == "gb300-mps"
+    assert abs(out["norm"] - 1.0) < 1e-10
+    assert abs(out["exp-val-z"] - dense.expect_z_parity(psi, [0, 3, 7])) < 1e-10
+
+
+@pytest.mark.gpu
+def test_plugin_sampling_and_itensor_mode():
+    circ = [("X", (0,), ()), ("CNOT", (0, 3), ())] + [("Measure", (q,), ()) for q in range(4)]
+    out = _run(4, 2000, circ, [("seed", 3), ("truncation-mode", "itensor")])
+    assert out["counts"] == {"1001": 2000}
+    # GHZ amplitude through the bitstring option (ITensorMPSVisitorTester.cpp:522-551)
+    g = [("H", (0,), ()), ("Z", (0,), ()), ("CNOT", (0, 1), ()), ("CNOT", (1, 2), ())]
+    psi = dense.run(3, g)
+    out = _run(3, 0, g, [("precision", "fp32")])
+    assert abs(out["norm"] - np.sum(np.abs(psi) ** 2)) < 1e-6

@@ -64,5 +64,25 @@ def build(verbose=False, force=False):
     return LIB
 
 
+VISITOR_DIR = os.path.join(HERE, "visitor")
+VISITOR_DEMO = os.path.join(OUT, "visitor_demo")
+
+
+def build_visitor_demo():
+    """Compile the C++ TNQVM visitor plugin (shim build) and its driver, linked
+    against libgb300mps.so."""
+    lib = build()
+    srcs = [os.path.join(VISITOR_DIR, f) for f in ("GpuMpsVisitor.cpp", "visitor_demo.cpp")]
+    deps = srcs + [os.path.join(VISITOR_DIR, f) for f in os.listdir(VISITOR_DIR) if f.endswith(".hpp")] + [lib]
+    if not _stale(VISITOR_DEMO, deps):
+        return VISITOR_DEMO
+    cmd = ["g++", "-std=c++17", "-O2", "-I", VISITOR_DIR] + srcs + ["-o", VISITOR_DEMO, "-L", OUT, "-lgb300mps",
+                                                                    "-Wl,-rpath," + OUT]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("visitor build failed: %s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr))
+    return VISITOR_DEMO
+
+
 if __name__ == "__main__":
     print(build(verbose="-v" in sys.argv, force="-f" in sys.argv))
