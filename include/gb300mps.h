@@ -174,6 +174,36 @@ int mps_serve_poll(mps_ctx* ctx, uint64_t ticket, int timeout_ms, double* energy
                    uint8_t* bits, double* latency_ms);
 int mps_serve_stop(mps_ctx* ctx);
 
+/* Allocation-free two-site update.  No counterpart in the reference: TNQVM's
+ * visitors always allocate through ExaTN/ITensor.  It exists for callers that
+ * cannot call cudaMalloc: code recording into a CUDA graph, processes whose
+ * device memory belongs to another allocator (a framework's memory pool), and
+ * latency-critical loops where an allocation's implicit synchronisation is not
+ * allowed.  It allocates nothing (no cudaMalloc/cudaFree, no allocating
+ * library call); its scratch is one file-scope device array of 256 B + 512 KiB
+ * that every GPU which loads this library holds until the process exits.
+ *
+ * The caller owns all inputs and outputs, in device memory:
+ *   sites      element buffer (complex128 or complex64 by precision) holding
+ *              the lo site (dl x 2 x dm, row-major) at element 0 and the hi
+ *              site (dm x 2 x dr) at element hi_offset; both are overwritten
+ *              in place with (dl x 2 x k) and (k x 2 x dr), so each region
+ *              needs room for k = min(2*dl, 2*dr, chi_max) on the new bond;
+ *   d_bonds    3 ints {dl, dm, dr}; d_bonds[1] receives k;
+ * and on the host: bonds (the same 3 ints, checked against the limit), the
+ * 4x4 gate (row = 2*phys(lo) + phys(hi)) and the stream to run on.
+ * exatn semantics split sqrt(S) onto both sites; itensor semantics leave the
+ * lo site left-isometric (the caller keeps the orthogonality centre on the
+ * pair).  Bonds above 64 are rejected with MPS_ERR_UNSUPPORTED.  The first
+ * call on a device looks up the array's device address and sets the kernel's
+ * shared-memory limit, so make that first call before any stream capture.
+ * Every call shares the one array and the call waits for its kernel, so two
+ * calls that overlap on the GPU (e.g. issued from two host threads on two
+ * streams) race on it. */
+int mps_gate2_apply_noalloc(int precision, int trunc_mode, int chi_max, double cutoff, void* sites,
+                            int64_t hi_offset, int* d_bonds, const int* bonds, const double gate[32],
+                            void* cuda_stream);
+
 /* Footprint used by admission: sum over sites of chi_l * 2 * chi_r * bytes. */
 size_t mps_footprint_bytes(int n_qubits, int chi_max, int precision);
 

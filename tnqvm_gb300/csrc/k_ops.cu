@@ -17,6 +17,10 @@
 // the projection W_k^H X (no division by singular values).
 #include <math.h>
 
+#include <cstring>
+#include <mutex>
+#include <string>
+
 #include "mps_common.cuh"
 
 namespace gbmps {
@@ -711,4 +715,126 @@ cudaError_t launch_ops(int prec, const ProgDesc* d_progs, int n_progs, int grid,
   return launch_ops_t<float>(d_progs, n_progs, grid, d_queue, scratch, st);
 }
 
+// ------------------------------------------------- allocation-free variant
+// Some callers cannot allocate device memory: code running inside a CUDA
+// stream capture that must not create allocations, hosts whose device memory
+// is owned by another allocator (a framework pool), or latency-critical
+// loops where cudaMalloc/cudaFree and their implicit synchronisation are
+// forbidden.  For them, mps_gate2_apply_noalloc runs one fused two-site
+// update with all of its scratch (theta, the FP64 eigenvector matrix, the
+// site offsets, statistics and the error word) in the file-scope array
+// below, which every GPU that loads this library holds until process exit.
+constexpr size_t kNoAllocHeader = 256;  // two site offsets, stats, error word
+constexpr size_t kNoAllocScratch = Layout<double>::scratch;  // largest per-CTA scratch (FP64)
+constexpr size_t kNoAllocBytes = kNoAllocHeader + kNoAllocScratch;  // 256 B + 512 KiB
+static __device__ __align__(256) char g_noalloc_scratch[kNoAllocBytes];
+
+template <typename T>
+__global__ void __launch_bounds__(kOpThreads, 1) k_gate2_noalloc(ProgDesc P, DevOp op, char* scratch) {
+  extern __shared__ __align__(16) char smem[];
+  SmallSmem<T>* sm = reinterpret_cast<SmallSmem<T>*>(smem + Layout<T>::big);
+  // the array keeps the previous call's contents: clear what must start at zero
+  if (threadIdx.x < ST_COUNT) P.stats[threadIdx.x] = 0.0;
+  if (threadIdx.x == 0) *P.err = 0;
+  __syncthreads();
+  op_gate2<T>(P, op, smem, sm, scratch);
+}
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+char* g_noalloc_ptr[kMaxDevices] = {nullptr};
+}  // namespace
+
+// Once per device, with that device current: the device address of the
+// array (its name in host code is only a stand-in) and the shared-memory
+// opt-in of the kernel.
+static int noalloc_setup(int dev, char** out) {
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    char* ptr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress((void**)&ptr, g_noalloc_scratch);
+    if (e != cudaSuccess) return 1;
+    e = cudaFuncSetAttribute(k_gate2_noalloc<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)Layout<float>::smem);
+    if (e != cudaSuccess) return 1;
+    e = cudaFuncSetAttribute(k_gate2_noalloc<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)Layout<double>::smem);
+    if (e != cudaSuccess) return 1;
+    g_noalloc_ptr[dev] = ptr;
+  }
+  *out = g_noalloc_ptr[dev];
+  return 0;
+}
+
 }  // namespace gbmps
+
+#include "../../include/gb300mps.h"
+
+namespace gbmps {
+int fail(int code, const std::string& msg);
+}
+
+extern "C" int mps_gate2_apply_noalloc(int precision, int trunc_mode, int chi_max, double cutoff, void* sites,
+                                       int64_t hi_offset, int* d_bonds, const int* bonds, const double gate[32],
+                                       void* cuda_stream) {
+  using namespace gbmps;
+  if (!sites || !d_bonds || !bonds || !gate) return fail(MPS_ERR_ARG, "NULL argument");
+  if (precision != MPS_PREC_FP64 && precision != MPS_PREC_FP32) return fail(MPS_ERR_ARG, "bad precision");
+  if (trunc_mode != MPS_TRUNC_EXATN && trunc_mode != MPS_TRUNC_ITENSOR) return fail(MPS_ERR_ARG, "bad trunc_mode");
+  for (int i = 0; i < 3; ++i)
+    if (bonds[i] < 1) return fail(MPS_ERR_ARG, "bond dimensions must be >= 1");
+  if (bonds[0] > kChiLimit || bonds[1] > kChiLimit || bonds[2] > kChiLimit)
+    return fail(MPS_ERR_UNSUPPORTED, "bond dimension above 64: the static scratch of the allocation-free "
+                                     "entry point holds one 128 x 128 theta (512 KiB)");
+  if (chi_max <= 0 || chi_max > kChiLimit) chi_max = kChiLimit;
+  if (cutoff < 0.0) cutoff = trunc_mode == MPS_TRUNC_EXATN ? 2.2250738585072014e-308 : 1e-6;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return fail(MPS_ERR_CUDA, cudaGetErrorString(e));
+  if (dev < 0 || dev >= kMaxDevices) return fail(MPS_ERR_UNSUPPORTED, "device ordinal too large");
+  char* base = nullptr;
+  if (noalloc_setup(dev, &base)) {
+    cudaGetLastError();
+    return fail(MPS_ERR_CUDA, "cudaGetSymbolAddress / cudaFuncSetAttribute failed for the static scratch");
+  }
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(cuda_stream);
+  // header: site offsets (2 x int64) at 0, stats (ST_COUNT doubles) at 64, error word at 192
+  const int64_t offs[2] = {0, hi_offset};
+  e = cudaMemcpyAsync(base, offs, sizeof(offs), cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return fail(MPS_ERR_CUDA, cudaGetErrorString(e));
+  ProgDesc P;
+  std::memset(&P, 0, sizeof(P));
+  P.sites = sites;
+  P.site_off = reinterpret_cast<const int64_t*>(base);
+  P.bond = d_bonds;
+  P.ops = nullptr;
+  P.n_ops = 1;
+  P.n = 2;
+  P.chi_cap = chi_max;
+  P.mode = trunc_mode;
+  P.flags = 0;
+  P.cutoff = cutoff;
+  P.stats = reinterpret_cast<double*>(base + 64);
+  P.err = reinterpret_cast<int*>(base + 192);
+  DevOp op;
+  std::memset(&op, 0, sizeof(op));
+  op.kind = OP_GATE2;
+  op.site = 0;
+  op.orient = trunc_mode == MPS_TRUNC_EXATN ? ORIENT_SQRT : ORIENT_TO_HI;
+  for (int i = 0; i < 32; ++i) op.m[i] = gate[i];
+  char* scratch = base + kNoAllocHeader;
+  if (precision == MPS_PREC_FP64)
+    k_gate2_noalloc<double><<<1, kOpThreads, Layout<double>::smem, st>>>(P, op, scratch);
+  else
+    k_gate2_noalloc<float><<<1, kOpThreads, Layout<float>::smem, st>>>(P, op, scratch);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(MPS_ERR_CUDA, cudaGetErrorString(e));
+  int herr = 0;
+  e = cudaMemcpyAsync(&herr, base + 192, sizeof(int), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return fail(MPS_ERR_CUDA, cudaGetErrorString(e));
+  if (herr & ERR_NAN) return fail(MPS_ERR_NUMERIC, "non-finite value in the two-site split");
+  if (herr & ERR_DIMS) return fail(MPS_ERR_UNSUPPORTED, "bond dimension beyond the kernel limit");
+  return MPS_OK;
+}

@@ -68,6 +68,8 @@ SIGNATURES = [
     ("mps_graph_destroy", _c.c_int, [_P]),
     ("mps_graph_timing", _c.c_int, [_P, _DP]),
     ("mps_gates", _c.c_int, [_P, _c.c_int, _c.POINTER(_c.c_int32), _c.POINTER(_c.c_int32), _DP]),
+    ("mps_gate2_apply_noalloc", _c.c_int, [_c.c_int, _c.c_int, _c.c_int, _c.c_double, _P, _c.c_int64,
+                                            _P, _c.POINTER(_c.c_int), _DP, _P]),
 ]
 
 GATE_IDS = {name: i for i, name in enumerate(
