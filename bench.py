@@ -217,6 +217,9 @@ def run_ours(args):
     clocks = clk.stop()
     ms = ev0.elapsed_time(ev1) / args.steps
     ops_ms, exp_ms, gemm_flops, eig_flops, op_bytes, res_bytes = g.timing()
+    cycles = g.phase_cycles()
+    cyc_total = sum(cycles.values()) or 1.0
+    phase_share = {k: v / cyc_total for k, v in cycles.items()}
     if dist is not None:
         t = torch.tensor([ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -274,6 +277,7 @@ def run_ours(args):
                          "note": "GEMM-class flops only (theta merge, gate, Gram, split); the Jacobi "
                                  "eigensolver runs on FP32 CUDA cores and dominates the kernel time"},
             "phases_ms": {"reset_plus_ops": ops_ms, "observables": exp_ms},
+            "fused_kernel_cycle_share": phase_share,
             "gpu_launches": 3 * args.steps,
             "clocks": clocks,
         }

@@ -159,6 +159,10 @@ int mps_graph_stream(mps_graph* g, void** cuda_stream);
  * bytes of the op table copied to the device by mps_graph_update, out[5]
  * bytes copied back per replay. */
 int mps_graph_timing(mps_graph* g, double out[6]);
+/* SM clock cycles of the last replay, summed over all programs, per phase of
+ * the fused update: out[0] theta, out[1] Gram, out[2] eigensolver, out[3]
+ * truncation + split, out[4] centre moves. */
+int mps_graph_phase_cycles(mps_graph* g, double out[5]);
 int mps_graph_destroy(mps_graph* g);
 
 /* Continuous-batching request loop (serving).  Requests are programs that

@@ -253,6 +253,19 @@ int mps_graph_timing(mps_graph* g, double out[6]) {
   return MPS_OK;
 }
 
+int mps_graph_phase_cycles(mps_graph* g, double out[5]) {
+  if (!g || !out) return fail(MPS_ERR_ARG, "NULL argument");
+  GCK(cudaSetDevice(g->c->device));
+  GCK(cudaStreamSynchronize(g->L.stream));
+  for (int i = 0; i < 5; ++i) out[i] = 0.0;
+  for (mps_prog* p : g->progs) {
+    double st[ST_COUNT];
+    GCK(cudaMemcpy(st, p->d_stats, sizeof(st), cudaMemcpyDeviceToHost));
+    for (int i = 0; i < 5; ++i) out[i] += st[ST_CYC_THETA + i];
+  }
+  return MPS_OK;
+}
+
 int mps_graph_stream(mps_graph* g, void** s) {
   if (!g || !s) return fail(MPS_ERR_ARG, "NULL argument");
   *s = (void*)g->L.stream;

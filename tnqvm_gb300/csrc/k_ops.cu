@@ -87,8 +87,11 @@ struct SmallSmem {
   int perm[kMaxM];
   T iso[kMaxM];
   T oth[kMaxM];
-  int rp_p[kMaxM / 2], rp_q[kMaxM / 2], rp_on[kMaxM / 2];
-  T rp_c[kMaxM / 2], rp_s[kMaxM / 2], rp_er[kMaxM / 2], rp_ei[kMaxM / 2];
+  int rp_p[kMaxM / 2], rp_q[kMaxM / 2];  // pairs of the current Jacobi step
+  int pos[kMaxM / 2];                    // slot of an active pair, -1 if it does not rotate
+  int sp[kMaxM / 2], sq[kMaxM / 2];      // per slot: the pair, its rotation c, s, e
+  T sc[kMaxM / 2], ss[kMaxM / 2];
+  cx<T> se[kMaxM / 2];
   cx<T> g[16];
   cx<T> tau[kChiLimit];
   double red[32];
@@ -100,7 +103,8 @@ template <typename T>
 struct Layout {
   // Large shared region: Gram (packed upper) [+ U for FP32], or the QR matrix + R.
   static constexpr size_t gram_bytes = sizeof(cx<T>) * (kMaxM * (kMaxM + 1) / 2);
-  static constexpr size_t u_bytes = Prec<T>::u_in_smem ? sizeof(cx<T>) * kMaxM * kMaxM : 0;
+  // U (m x m), or X staged for the Gram with a padded stride (m x (m+1))
+  static constexpr size_t u_bytes = Prec<T>::u_in_smem ? sizeof(cx<T>) * kMaxM * (kMaxM + 1) : 0;
   static constexpr size_t qr_bytes = sizeof(cx<T>) * (kMaxM * kChiLimit + kChiLimit * kChiLimit);
   static constexpr size_t big = (gram_bytes + u_bytes) > qr_bytes ? (gram_bytes + u_bytes) : qr_bytes;
   static constexpr size_t smem = big + sizeof(SmallSmem<T>);
@@ -126,101 +130,103 @@ __device__ int jacobi_eigh(cx<T>* Gp, cx<T>* U, int m, double trace, SmallSmem<T
   // absolute eps*trace floor leaves off-diagonals that mix kept and discarded
   // eigenvectors across small gaps and costs accuracy after truncation.
   const T tol_abs = T(64.0 * Prec<T>::eps * Prec<T>::eps * trace);
+  // Two per-step counters of active rotations, alternating with a global step
+  // index: the counter of step s+1 is cleared during step s's rotation phase,
+  // which every thread reaches only after all have read the count of step s-1
+  // (or that count was zero, in which case clearing it changes nothing).
+  if (tid == 0) {
+    sm->ival[3] = 0;
+    sm->ival[4] = 0;
+  }
+  __syncthreads();
+  int gs = 0;
   for (int sweep = 0; sweep < Prec<T>::max_sweeps; ++sweep) {
-    if (tid == 0) sm->ival[0] = 0;
-    __syncthreads();
-    for (int r = 0; r < m - 1; ++r) {
+    int nrot = 0;
+    for (int r = 0; r < m - 1; ++r, ++gs) {
+      int* cnt = &sm->ival[3 + (gs & 1)];
+      if (tid == 0) sm->ival[3 + ((gs + 1) & 1)] = 0;
+      // Rotation of each pair j: J = [[c, s], [-s e*, c e*]] with e = g/|g|,
+      // listed compactly by slot for the update phase.
       for (int j = tid; j < np; j += nt) {
         int p, q;
         rr_pair(m, r, j, p, q);
         const T a = Gp[pidx(p, p, m)].re, b = Gp[pidx(q, q, m)].re;
         const cx<T> g = gget(Gp, p, q, m);
         const T ag = sqrt(abs2(g));
-        int on = 0;
-        T c = T(1), s = T(0), er = T(1), ei = T(0);
-        if (ag > tol_abs && ag > tol_rel * sqrt(fabs(a * b))) {
-          on = 1;
-          er = g.re / ag;
-          ei = g.im / ag;
-          const T zeta = (b - a) / (T(2) * ag);
-          const T tt = (zeta >= T(0) ? T(1) : T(-1)) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
-          c = T(1) / sqrt(T(1) + tt * tt);
-          s = c * tt;
-          atomicAdd(&sm->ival[0], 1);
-        }
         sm->rp_p[j] = p;
         sm->rp_q[j] = q;
-        sm->rp_on[j] = on;
-        sm->rp_c[j] = c;
-        sm->rp_s[j] = s;
-        sm->rp_er[j] = er;
-        sm->rp_ei[j] = ei;
+        if (ag > tol_abs && ag > tol_rel * sqrt(fabs(a * b))) {
+          const T zeta = (b - a) / (T(2) * ag);
+          const T tt = (zeta >= T(0) ? T(1) : T(-1)) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
+          const T c = T(1) / sqrt(T(1) + tt * tt);
+          const int slot = atomicAdd(cnt, 1);
+          sm->pos[j] = slot;
+          sm->sp[slot] = p;
+          sm->sq[slot] = q;
+          sm->sc[slot] = c;
+          sm->ss[slot] = c * tt;
+          sm->se[slot] = mk<T>(g.re / ag, g.im / ag);
+        } else {
+          sm->pos[j] = -1;
+        }
       }
       __syncthreads();
-      // G <- J^H G J as independent 2x2 block updates over pair blocks I <= J.
-      for (int t = tid; t < np * np; t += nt) {
-        const int I = t / np, J = t - I * np;
-        if (I > J) continue;
-        const int onI = sm->rp_on[I], onJ = sm->rp_on[J];
-        if (!onI && !onJ) continue;
-        const int pI = sm->rp_p[I], qI = sm->rp_q[I], pJ = sm->rp_p[J], qJ = sm->rp_q[J];
-        // J = [[c, s], [-s e*, c e*]]
-        cx<T> jI00 = mk<T>(sm->rp_c[I], 0), jI01 = mk<T>(sm->rp_s[I], 0);
-        cx<T> eIc = mk<T>(sm->rp_er[I], -sm->rp_ei[I]);
-        cx<T> jI10 = scl(eIc, -sm->rp_s[I]), jI11 = scl(eIc, sm->rp_c[I]);
-        cx<T> jJ00 = mk<T>(sm->rp_c[J], 0), jJ01 = mk<T>(sm->rp_s[J], 0);
-        cx<T> eJc = mk<T>(sm->rp_er[J], -sm->rp_ei[J]);
-        cx<T> jJ10 = scl(eJc, -sm->rp_s[J]), jJ11 = scl(eJc, sm->rp_c[J]);
-        if (I == J) {
+      const int na = *cnt;
+      nrot += na;
+      if (na == 0) continue;  // nothing rotates: G and U unchanged, no second barrier needed
+      // G <- J^H G J as independent 2x2 block updates over the pair blocks
+      // that touch an active rotation; a block of two active pairs is done
+      // once, by the one in the lower slot.
+      for (int t = tid; t < na * np; t += nt) {
+        const int ai = t / np, J = t - ai * np;
+        const int bj = sm->pos[J];
+        if (bj >= 0 && bj < ai) continue;
+        const int pI = sm->sp[ai], qI = sm->sq[ai];
+        const T cI = sm->sc[ai], sI = sm->ss[ai];
+        const cx<T> eI = sm->se[ai];
+        if (bj == ai) {  // diagonal block: the rotation zeroes G[p][q]
           const T a = Gp[pidx(pI, pI, m)].re, b = Gp[pidx(qI, qI, m)].re;
           const cx<T> g = gget(Gp, pI, qI, m);
-          // diag(J^H B J): a' = |j00|^2 a + |j10|^2 b + 2 Re(conj(j00) g j10)
-          const cx<T> x = conj(jI00) * g * jI10;
-          const cx<T> y = conj(jI01) * g * jI11;
-          const T an = abs2(jI00) * a + abs2(jI10) * b + T(2) * x.re;
-          const T bn = abs2(jI01) * a + abs2(jI11) * b + T(2) * y.re;
+          // diag(J^H B J) with |g| = Re(g e*): a' = a - 2cs|g| ... written out
+          const T gr = g.re * eI.re + g.im * eI.im;
+          const T an = cI * cI * a + sI * sI * b - T(2) * cI * sI * gr;
+          const T bn = sI * sI * a + cI * cI * b + T(2) * cI * sI * gr;
           Gp[pidx(pI, pI, m)] = mk<T>(an, 0);
           Gp[pidx(qI, qI, m)] = mk<T>(bn, 0);
           gset(Gp, pI, qI, m, mk<T>(0, 0));
           continue;
         }
+        const int pJ = sm->rp_p[J], qJ = sm->rp_q[J];
         const cx<T> b00 = gget(Gp, pI, pJ, m), b01 = gget(Gp, pI, qJ, m);
         const cx<T> b10 = gget(Gp, qI, pJ, m), b11 = gget(Gp, qI, qJ, m);
         cx<T> c00 = b00, c01 = b01, c10 = b10, c11 = b11;
-        if (onJ) {  // B J
-          c00 = b00 * jJ00 + b01 * jJ10;
-          c01 = b00 * jJ01 + b01 * jJ11;
-          c10 = b10 * jJ00 + b11 * jJ10;
-          c11 = b10 * jJ01 + b11 * jJ11;
+        if (bj >= 0) {  // C = B J
+          const T cJ = sm->sc[bj], sJ = sm->ss[bj];
+          const cx<T> eJc = conj(sm->se[bj]);
+          const cx<T> u0 = b01 * eJc, u1 = b11 * eJc;
+          c00 = scl(b00, cJ) - scl(u0, sJ);
+          c01 = scl(b00, sJ) + scl(u0, cJ);
+          c10 = scl(b10, cJ) - scl(u1, sJ);
+          c11 = scl(b10, sJ) + scl(u1, cJ);
         }
-        cx<T> d00 = c00, d01 = c01, d10 = c10, d11 = c11;
-        if (onI) {  // J^H (B J)
-          d00 = conj(jI00) * c00 + conj(jI10) * c10;
-          d01 = conj(jI00) * c01 + conj(jI10) * c11;
-          d10 = conj(jI01) * c00 + conj(jI11) * c10;
-          d11 = conj(jI01) * c01 + conj(jI11) * c11;
-        }
-        gset(Gp, pI, pJ, m, d00);
-        gset(Gp, pI, qJ, m, d01);
-        gset(Gp, qI, pJ, m, d10);
-        gset(Gp, qI, qJ, m, d11);
+        // D = J^H C, J^H = [[c, -s e], [s, c e]]
+        const cx<T> v0 = eI * c10, v1 = eI * c11;
+        gset(Gp, pI, pJ, m, scl(c00, cI) - scl(v0, sI));
+        gset(Gp, pI, qJ, m, scl(c01, cI) - scl(v1, sI));
+        gset(Gp, qI, pJ, m, scl(c00, sI) + scl(v0, cI));
+        gset(Gp, qI, qJ, m, scl(c01, sI) + scl(v1, cI));
       }
-      // U <- U J
-      for (int t = tid; t < m * np; t += nt) {
-        const int row = t / np, j = t - row * np;
-        if (!sm->rp_on[j]) continue;
-        const int p = sm->rp_p[j], q = sm->rp_q[j];
-        const T c = sm->rp_c[j], s = sm->rp_s[j];
-        const cx<T> ec = mk<T>(sm->rp_er[j], -sm->rp_ei[j]);
-        const cx<T> up = U[row * m + p], uq = U[row * m + q];
-        const cx<T> uqe = uq * ec;
+      // U <- U J on the columns of the active pairs
+      for (int t = tid; t < m * na; t += nt) {
+        const int row = t / na, a = t - row * na;
+        const int p = sm->sp[a], q = sm->sq[a];
+        const T c = sm->sc[a], s = sm->ss[a];
+        const cx<T> up = U[row * m + p], uqe = U[row * m + q] * conj(sm->se[a]);
         U[row * m + p] = scl(up, c) - scl(uqe, s);
         U[row * m + q] = scl(up, s) + scl(uqe, c);
       }
       __syncthreads();
     }
-    const int nrot = sm->ival[0];
-    __syncthreads();
     total_rot += nrot;
     if (nrot == 0) break;
   }
@@ -343,6 +349,7 @@ __device__ void op_gate2(const ProgDesc& P, const DevOp& op, char* big, SmallSme
   cx<T>* B = sites + P.site_off[lo + 1];
   const int R = 2 * dl, Cc = 2 * dr;
   cx<T>* Th = reinterpret_cast<cx<T>*>(scratch);
+  const long long c_start = clock64();
   if (tid < 16) sm->g[tid] = mk<T>(T(op.m[2 * tid]), T(op.m[2 * tid + 1]));
   __syncthreads();
   // theta[(l,p1),(p2,r)] = sum_{q1,q2} G[2p1+p2][2q1+q2] sum_m A[l,q1,m] B[m,q2,r]
@@ -381,20 +388,87 @@ __device__ void op_gate2(const ProgDesc& P, const DevOp& op, char* big, SmallSme
   cx<T>* Gp = reinterpret_cast<cx<T>*>(big);
   cx<T>* U = Prec<T>::u_in_smem ? reinterpret_cast<cx<T>*>(big + Layout<T>::gram_bytes)
                                 : reinterpret_cast<cx<T>*>(scratch + sizeof(cx<T>) * kMaxM * kMaxM);
+  const long long c_theta = clock64();
   double tr_part = 0.0;
-  for (int t = tid; t < m * m; t += nt) {
-    const int i = t / m, j = t - i * m;
-    if (i > j) continue;
-    cx<T> acc = mk<T>(0, 0);
-    for (int c = 0; c < nn; ++c) fma_c(acc, X(i, c), conj(X(j, c)));
-    if (i == j) {
-      acc.im = T(0);
-      tr_part += (double)acc.re;
+  if (Prec<T>::u_in_smem) {
+    // Stage X (m x nn) in the U region with a padded row stride, then form
+    // the upper triangle of G = X X^H in 4x4 register tiles.
+    cx<T>* Xs = U;
+    const int ld = nn + 1;
+    for (int t = tid; t < m * nn; t += nt) {
+      if (!tr) {
+        const int i = t / nn, c = t - i * nn;
+        Xs[i * ld + c] = Th[i * Cc + c];
+      } else {
+        const int c = t / m, i = t - c * m;
+        Xs[i * ld + c] = Th[c * Cc + i];
+      }
     }
-    Gp[pidx(i, j, m)] = acc;
+    __syncthreads();
+    const int nb = (m + 3) >> 2;
+    const int ntiles = nb * (nb + 1) / 2;
+    for (int tt = tid; tt < ntiles; tt += nt) {
+      int bi = 0, rem = tt;
+      while (rem >= nb - bi) {
+        rem -= nb - bi;
+        ++bi;
+      }
+      const int bj = bi + rem;
+      int ri[4], rj[4];
+#pragma unroll
+      for (int a = 0; a < 4; ++a) {
+        ri[a] = min(4 * bi + a, m - 1) * ld;
+        rj[a] = min(4 * bj + a, m - 1) * ld;
+      }
+      cx<T> acc[4][4];
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) acc[a][b] = mk<T>(0, 0);
+      for (int c = 0; c < nn; ++c) {
+        cx<T> xi[4], xj[4];
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+          xi[a] = Xs[ri[a] + c];
+          xj[a] = Xs[rj[a] + c];
+        }
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+          for (int b = 0; b < 4; ++b) fma_c(acc[a][b], xi[a], conj(xj[b]));
+      }
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+          const int i = 4 * bi + a, j = 4 * bj + b;
+          if (i < m && j < m && i <= j) {
+            cx<T> v = acc[a][b];
+            if (i == j) {
+              v.im = T(0);
+              tr_part += (double)v.re;
+            }
+            Gp[pidx(i, j, m)] = v;
+          }
+        }
+    }
+  } else {
+    for (int t = tid; t < m * m; t += nt) {
+      const int i = t / m, j = t - i * m;
+      if (i > j) continue;
+      cx<T> acc = mk<T>(0, 0);
+      for (int c = 0; c < nn; ++c) fma_c(acc, X(i, c), conj(X(j, c)));
+      if (i == j) {
+        acc.im = T(0);
+        tr_part += (double)acc.re;
+      }
+      Gp[pidx(i, j, m)] = acc;
+    }
   }
   const double trace = block_sum(tr_part, sm->red);
+  const long long c_gram = clock64();
   const int nrot_total = jacobi_eigh<T>(Gp, U, m, trace, sm);
+  const long long c_eig = clock64();
   // eigenvalues, descending order
   for (int i = tid; i < m; i += nt) sm->lam[i] = (double)Gp[pidx(i, i, m)].re;
   __syncthreads();
@@ -557,7 +631,14 @@ __device__ void op_gate2(const ProgDesc& P, const DevOp& op, char* big, SmallSme
       B[j * Cc + i] = w;  // hi site (k, 2, dr)
   }
   __syncthreads();
-  if (tid == 0) P.bond[lo + 1] = k;
+  if (tid == 0) {
+    P.bond[lo + 1] = k;
+    const long long c_end = clock64();
+    P.stats[ST_CYC_THETA] += (double)(c_theta - c_start);
+    P.stats[ST_CYC_GRAM] += (double)(c_gram - c_theta);
+    P.stats[ST_CYC_EIG] += (double)(c_eig - c_gram);
+    P.stats[ST_CYC_SPLIT] += (double)(c_end - c_eig);
+  }
 }
 
 // Centre move to the right: A_c = Q R (rows (l,p)), A_{c+1} <- R A_{c+1}.
@@ -565,6 +646,7 @@ template <typename T>
 __device__ void op_move_r(const ProgDesc& P, const DevOp& op, char* big, SmallSmem<T>* sm, char* scratch) {
   const int tid = threadIdx.x, nt = blockDim.x;
   const int c = op.site;
+  const long long c_start = clock64();
   const int dl = P.bond[c], dr = P.bond[c + 1], dr2 = P.bond[c + 2];
   if (2 * dl > kMaxM || dr > kChiLimit) {
     if (tid == 0) atomicOr(P.err, ERR_DIMS);
@@ -599,6 +681,7 @@ __device__ void op_move_r(const ProgDesc& P, const DevOp& op, char* big, SmallSm
     P.bond[c + 1] = k;
     P.stats[ST_FLOPS] += 4.0 * k * nc * w;
     P.stats[ST_EIG_FLOPS] += 32.0 * mr * nc * nc;
+    P.stats[ST_CYC_MOVE] += (double)(clock64() - c_start);
   }
 }
 
@@ -607,6 +690,7 @@ template <typename T>
 __device__ void op_move_l(const ProgDesc& P, const DevOp& op, char* big, SmallSmem<T>* sm, char* scratch) {
   const int tid = threadIdx.x, nt = blockDim.x;
   const int c = op.site;
+  const long long c_start = clock64();
   const int dl = P.bond[c], dr = P.bond[c + 1], dl2 = P.bond[c - 1];
   if (2 * dr > kMaxM || dl > kChiLimit) {
     if (tid == 0) atomicOr(P.err, ERR_DIMS);
@@ -644,6 +728,7 @@ __device__ void op_move_l(const ProgDesc& P, const DevOp& op, char* big, SmallSm
     P.bond[c] = k;
     P.stats[ST_FLOPS] += 4.0 * k * nc * h;
     P.stats[ST_EIG_FLOPS] += 32.0 * mr * nc * nc;
+    P.stats[ST_CYC_MOVE] += (double)(clock64() - c_start);
   }
 }
 

@@ -88,7 +88,12 @@ enum StatSlot {
   ST_N_OPS = 3,       // number of ops executed
   ST_FLOPS = 4,       // GEMM-class flops: theta merge + gate + Gram + split + centre-move products
   ST_EIG_FLOPS = 5,   // Jacobi rotations and Householder reflections
-  ST_COUNT = 6,
+  ST_CYC_THETA = 6,   // SM clock cycles spent per phase (thread 0's clock64 deltas)
+  ST_CYC_GRAM = 7,
+  ST_CYC_EIG = 8,
+  ST_CYC_SPLIT = 9,
+  ST_CYC_MOVE = 10,
+  ST_COUNT = 11,
 };
 
 // Error bits written by the kernels into ProgDesc::err.

@@ -67,6 +67,7 @@ SIGNATURES = [
     ("mps_graph_stream", _c.c_int, [_P, _c.POINTER(_P)]),
     ("mps_graph_destroy", _c.c_int, [_P]),
     ("mps_graph_timing", _c.c_int, [_P, _DP]),
+    ("mps_graph_phase_cycles", _c.c_int, [_P, _DP]),
     ("mps_gates", _c.c_int, [_P, _c.c_int, _c.POINTER(_c.c_int32), _c.POINTER(_c.c_int32), _DP]),
     ("mps_gate2_apply_noalloc", _c.c_int, [_c.c_int, _c.c_int, _c.c_int, _c.c_double, _P, _c.c_int64,
                                             _P, _c.POINTER(_c.c_int), _DP, _P]),
@@ -231,6 +232,12 @@ class Graph:
         out = np.zeros(6)
         _check(_lib.mps_graph_timing(self.h, _dptr(out)))
         return tuple(out)
+
+    def phase_cycles(self):
+        """SM cycles of the last replay per phase: theta, Gram, eigensolver, split, centre moves."""
+        out = np.zeros(5)
+        _check(_lib.mps_graph_phase_cycles(self.h, _dptr(out)))
+        return dict(zip(["theta", "gram", "eigensolver", "split", "moves"], out.tolist()))
 
     @property
     def stream(self):
