@@ -94,6 +94,14 @@ struct SmallSmem {
   cx<T> se[kMaxM / 2];
   cx<T> g[16];
   cx<T> tau[kChiLimit];
+  // tridiagonal eigensolver (FP32 path)
+  cx<T> ttau[kMaxM];     // Householder scalars of the tridiagonalisation
+  cx<T> tv[kMaxM];       // current reflector v
+  cx<T> tp[kMaxM];       // p = tau A v, then w
+  cx<T> twv[kMaxM];      // v^H W during the back-transform
+  T td[kMaxM], te[kMaxM];  // tridiagonal: diagonal, off-diagonal
+  int bs[kMaxM], bt[kMaxM];  // unreduced block [bs, bt] containing each row
+  double lk[kMaxM];  // eigenvalues of the kept-column order (head, then refined tail)
   double red[32];
   int ival[8];
   double dval[8];
@@ -108,9 +116,16 @@ struct Layout {
   static constexpr size_t qr_bytes = sizeof(cx<T>) * (kMaxM * kChiLimit + kChiLimit * kChiLimit);
   static constexpr size_t big = (gram_bytes + u_bytes) > qr_bytes ? (gram_bytes + u_bytes) : qr_bytes;
   static constexpr size_t smem = big + sizeof(SmallSmem<T>);
-  // Global scratch per CTA: theta, and U for FP64.
-  static constexpr size_t scratch = sizeof(cx<T>) * kMaxM * kMaxM * (Prec<T>::u_in_smem ? 1 : 2);
+  // Global scratch per CTA: theta, then U for FP64, or for FP32 two m x chi
+  // blocks (the refinement's head vectors, then the subspace step's X^H W).
+  static constexpr size_t scratch =
+      sizeof(cx<T>) * (kMaxM * kMaxM + (Prec<T>::u_in_smem ? 2 * kMaxM * kChiLimit : kMaxM * kMaxM));
 };
+
+// FP32 refinement threshold: eigenvalues below this fraction of the largest
+// form the tail that is re-solved (singular-value ratio 1e-2; the FP32 Gram's
+// absolute error is ~1e-7 of the trace).
+constexpr double kRefineRatio = 1e-4;
 
 // ------------------------------------------------------------------ Jacobi
 // Diagonalise the m x m Hermitian matrix held packed in Gp; U (ld = m)
@@ -264,8 +279,12 @@ __device__ void householder_qr(cx<T>* M, int mr, int nc, cx<T>* Rb, SmallSmem<T>
     }
     __syncthreads();
     if (sm->ival[1]) {
-      const cx<T> inv = mk<T>(T(sm->dval[0]), T(sm->dval[1]));
-      for (int i = j + 1 + tid; i < mr; i += nt) M[i * nc + j] = M[i * nc + j] * inv;
+      // scale in double: 1/(alpha - beta) can exceed the range of T
+      const double ir = sm->dval[0], ii = sm->dval[1];
+      for (int i = j + 1 + tid; i < mr; i += nt) {
+        const cx<T> x = M[i * nc + j];
+        M[i * nc + j] = mk<T>(T((double)x.re * ir - (double)x.im * ii), T((double)x.re * ii + (double)x.im * ir));
+      }
       __syncthreads();
       const cx<T> ctau = conj(sm->tau[j]);
       for (int c = j + 1 + warp; c < nc; c += nw) {
@@ -317,6 +336,454 @@ __device__ void householder_qr(cx<T>* M, int mr, int nc, cx<T>* Rb, SmallSmem<T>
     }
     __syncthreads();
   }
+}
+
+// ------------------------------------------------- tridiagonal eigensolver
+// FP32 path of the Gram eigen-decomposition, ~10x fewer flops than Jacobi:
+// Householder reduction to real symmetric tridiagonal form, eigenvalues of
+// each unreduced block by multisection bisection (Sturm counts), the kept
+// eigenvectors by one twisted factorisation each (Dhillon-Parlett), and the
+// back-transform by the stored reflectors.
+
+// A: full Hermitian m x m (ld m) in shared memory.  On return td/te hold the
+// tridiagonal T = Q^H A Q, Q = H_0 ... H_{m-2}, H_j = I - ttau[j] v_j v_j^H with
+// v_j[j+1] = 1 and v_j[i] (i > j+1) stored in A[i][j] (LAPACK zhetd2, lower).
+template <typename T>
+__device__ void tridiagonalize(cx<T>* A, int m, double trace, SmallSmem<T>* sm) {
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
+  // columns this small relative to the trace are flushed to zero, so the
+  // reflector scale 1/(alpha - beta) stays finite in T
+  const double flush2 = 1e-60 * trace * trace + 1e-74;
+  for (int j = 0; j + 1 < m; ++j) {
+    const int L = m - j - 1;  // x = A[j+1:m, j]
+    if (warp == 0) {
+      double s = 0.0;
+      for (int i = 1 + lane; i < L; i += 32) s += (double)abs2(A[(j + 1 + i) * m + j]);
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      const cx<T> alpha = A[(j + 1) * m + j];
+      double ar = alpha.re, ai = alpha.im;
+      double nrm2 = ar * ar + ai * ai + s;
+      const bool flush = nrm2 <= flush2;
+      if (flush) {
+        ar = ai = s = nrm2 = 0.0;
+      }
+      double beta = ar, tr = 0.0, ti = 0.0, ir = 0.0, ii = 0.0;
+      const bool refl = !((s == 0.0 && ai == 0.0) || nrm2 == 0.0);
+      if (refl) {
+        beta = -copysign(sqrt(nrm2), ar);
+        tr = (beta - ar) / beta;
+        ti = -ai / beta;
+        const double dr = ar - beta, di = ai, den = dr * dr + di * di;
+        ir = dr / den;
+        ii = -di / den;
+      }
+      for (int i = lane; i < L; i += 32) {
+        cx<T> v = mk<T>(T(i == 0), T(0));
+        if (i > 0 && refl && !flush) {
+          const cx<T> x = A[(j + 1 + i) * m + j];
+          v = mk<T>(T((double)x.re * ir - (double)x.im * ii), T((double)x.re * ii + (double)x.im * ir));
+        }
+        sm->tv[i] = v;
+      }
+      if (lane == 0) {
+        sm->ttau[j] = mk<T>(T(tr), T(ti));
+        sm->te[j] = T(beta);
+      }
+    }
+    __syncthreads();
+    const cx<T> tau = sm->ttau[j];
+    for (int i = tid; i < L; i += nt) A[(j + 1 + i) * m + j] = i == 0 ? mk<T>(sm->te[j], 0) : sm->tv[i];
+    if (tau.re == T(0) && tau.im == T(0)) {
+      __syncthreads();
+      continue;
+    }
+    // p = tau * At v with At = A[j+1:, j+1:]; four lanes per row
+    {
+      const int r = tid >> 2, q = tid & 3;
+      cx<T> acc = mk<T>(0, 0);
+      if (r < L) {
+        const cx<T>* row = A + (j + 1 + r) * m + (j + 1);
+        for (int c = q; c < L; c += 4) fma_c(acc, row[c], sm->tv[c]);
+      }
+      acc.re += __shfl_xor_sync(0xffffffffu, acc.re, 1);
+      acc.im += __shfl_xor_sync(0xffffffffu, acc.im, 1);
+      acc.re += __shfl_xor_sync(0xffffffffu, acc.re, 2);
+      acc.im += __shfl_xor_sync(0xffffffffu, acc.im, 2);
+      if (r < L && q == 0) sm->tp[r] = tau * acc;
+    }
+    __syncthreads();
+    // w = p - 1/2 tau (p^H v) v
+    if (warp == 0) {
+      cx<T> d = mk<T>(0, 0);
+      for (int i = lane; i < L; i += 32) fma_cj(d, sm->tp[i], sm->tv[i]);
+      for (int o = 16; o > 0; o >>= 1) {
+        d.re += __shfl_xor_sync(0xffffffffu, d.re, o);
+        d.im += __shfl_xor_sync(0xffffffffu, d.im, o);
+      }
+      const cx<T> a2 = scl(tau * d, T(-0.5));
+      __syncwarp();
+      for (int i = lane; i < L; i += 32) sm->tp[i] = sm->tp[i] + a2 * sm->tv[i];
+    }
+    __syncthreads();
+    // At -= v w^H + w v^H
+    for (int t = tid; t < L * L; t += nt) {
+      const int r = t / L, c = t - r * L;
+      cx<T>& a = A[(j + 1 + r) * m + (j + 1 + c)];
+      a = a - (sm->tv[r] * conj(sm->tp[c]) + sm->tp[r] * conj(sm->tv[c]));
+    }
+    __syncthreads();
+  }
+  for (int i = tid; i < m; i += nt) sm->td[i] = A[i * m + i].re;
+  __syncthreads();
+}
+
+// All eigenvalues of T (td, te): split into unreduced blocks, then each row j
+// finds the (j - block start)-th smallest eigenvalue of its block with four
+// lanes multisecting the interval (16 rounds of 5-section, fixed count).
+// Results: sm->lam[j] and the block bounds sm->bs[j], sm->bt[j].
+template <typename T>
+__device__ void tri_bisect(int m, SmallSmem<T>* sm) {
+  const int tid = threadIdx.x;
+  const T eps = T(Prec<T>::eps);
+  if (tid == 0) {
+    int s = 0;
+    for (int i = 0; i < m; ++i) {
+      bool split = i == m - 1;
+      if (!split) {
+        const T e = fabs(sm->te[i]);
+        if (e <= eps * (fabs(sm->td[i]) + fabs(sm->td[i + 1]))) {
+          split = true;
+          sm->te[i] = T(0);
+        }
+      }
+      if (split) {
+        for (int r = s; r <= i; ++r) {
+          sm->bs[r] = s;
+          sm->bt[r] = i;
+        }
+        s = i + 1;
+      }
+    }
+  }
+  __syncthreads();
+  const int j = tid >> 2, q = tid & 3;
+  const bool live = j < m;
+  const int s = live ? sm->bs[j] : 0, t = live ? sm->bt[j] : -1;
+  const int local = j - s;
+  T lo = T(0), hi = T(0), maxe2 = T(1);
+  for (int i = s; i <= t; ++i) {
+    const T el = i > s ? fabs(sm->te[i - 1]) : T(0), er = i < t ? fabs(sm->te[i]) : T(0);
+    const T d = sm->td[i];
+    if (i == s) {
+      lo = d - el - er;
+      hi = d + el + er;
+    } else {
+      lo = fmin(lo, d - el - er);
+      hi = fmax(hi, d + el + er);
+    }
+    maxe2 = fmax(maxe2, er * er);
+  }
+  const T pivmin = T(1.2e-38) * maxe2;
+  const T pad = T(4) * eps * fmax(fabs(lo), fabs(hi)) + pivmin;
+  T a = lo - pad, b = hi + pad;
+  const unsigned gmask = 0xFu << (threadIdx.x & 28);
+  for (int round = 0; round < 16; ++round) {
+    const T w = (b - a) / T(5);
+    const T x = a + w * T(q + 1);
+    int cnt = 0;
+    T qv = T(1);
+    for (int i = s; i <= t; ++i) {
+      const T e2 = i > s ? sm->te[i - 1] * sm->te[i - 1] : T(0);
+      qv = (sm->td[i] - x) - (i > s ? e2 / qv : T(0));
+      if (fabs(qv) < pivmin) qv = -pivmin;
+      cnt += qv < T(0);
+    }
+    const int base = threadIdx.x & 31 & ~3;
+    const int c0 = __shfl_sync(gmask, cnt, base + 0), c1 = __shfl_sync(gmask, cnt, base + 1);
+    const int c2 = __shfl_sync(gmask, cnt, base + 2), c3 = __shfl_sync(gmask, cnt, base + 3);
+    const T x0 = a + w * T(1), x1 = a + w * T(2), x2 = a + w * T(3), x3 = a + w * T(4);
+    if (c0 > local) {
+      b = x0;
+    } else if (c1 > local) {
+      a = x0;
+      b = x1;
+    } else if (c2 > local) {
+      a = x1;
+      b = x2;
+    } else if (c3 > local) {
+      a = x2;
+      b = x3;
+    } else {
+      a = x3;
+    }
+  }
+  if (live && q == 0) sm->lam[j] = (double)(T(0.5) * (a + b));
+  __syncthreads();
+}
+
+// Twisted-factorisation eigenvector of T for eigenvalue lam on block [s, t],
+// written into column c of W (m x k, ld k); real parts first hold D+ and
+// imaginary parts D- of the two factorisations, then the vector.
+template <typename T>
+__device__ void tri_twisted(cx<T>* W, int m, int k, int c, T lam, int s, int t, SmallSmem<T>* sm) {
+  // Pivots are kept at least eps*|T| (block scale) away from zero, so one
+  // step of the vector recurrence grows a component by at most ~1/eps^2; the
+  // partial vector is rescaled whenever a component passes 1e15, so neither
+  // the components nor their squared norm overflow.
+  T scale = T(0);
+  for (int i = s; i <= t; ++i) scale = fmax(scale, fabs(sm->td[i] - lam) + (i < t ? fabs(sm->te[i]) : T(0)));
+  const T tiny = fmax(T(Prec<T>::eps) * T(Prec<T>::eps) * scale, T(1e-35));
+  auto guard = [&](T v) { return fabs(v) < tiny ? -tiny : v; };
+  W[s * k + c].re = sm->td[s] - lam;
+  for (int i = s + 1; i <= t; ++i) {
+    const T e = sm->te[i - 1];
+    W[i * k + c].re = (sm->td[i] - lam) - e * e / guard(W[(i - 1) * k + c].re);
+  }
+  W[t * k + c].im = sm->td[t] - lam;
+  for (int i = t - 1; i >= s; --i) {
+    const T e = sm->te[i];
+    W[i * k + c].im = (sm->td[i] - lam) - e * e / guard(W[(i + 1) * k + c].im);
+  }
+  int r = s;
+  T best = T(3.0e38);
+  for (int i = s; i <= t; ++i) {
+    const T g = fabs(W[i * k + c].re + W[i * k + c].im - (sm->td[i] - lam));
+    if (g < best) {
+      best = g;
+      r = i;
+    }
+  }
+  const T big = T(1e15), shrink = T(1e-15);
+  T nrm = T(1);
+  W[r * k + c].re = T(1);
+  int lo_done = r;
+  for (int i = r - 1; i >= s; --i) {
+    T z = -(sm->te[i] / guard(W[i * k + c].re)) * W[(i + 1) * k + c].re;
+    if (fabs(z) > big) {  // rescale what is computed so far: rows i+1..r
+      for (int u = i + 1; u <= r; ++u) W[u * k + c].re *= shrink;
+      nrm *= shrink * shrink;
+      z *= shrink;
+    }
+    W[i * k + c].re = z;
+    nrm += z * z;
+    lo_done = i;
+  }
+  for (int i = r + 1; i <= t; ++i) {
+    T z = -(sm->te[i - 1] / guard(W[i * k + c].im)) * W[(i - 1) * k + c].re;
+    if (fabs(z) > big) {  // rows lo_done..i-1
+      for (int u = lo_done; u < i; ++u) W[u * k + c].re *= shrink;
+      nrm *= shrink * shrink;
+      z *= shrink;
+    }
+    W[i * k + c].re = z;
+    nrm += z * z;
+  }
+  const T inv = T(1) / sqrt(nrm);
+  for (int i = 0; i < m; ++i) {
+    const bool in = i >= s && i <= t;
+    W[i * k + c] = mk<T>(in ? W[i * k + c].re * inv : T(0), T(0));
+  }
+}
+
+// W <- Q W with the reflectors left in A by tridiagonalize (W: m x k, ld ld).
+template <typename T>
+__device__ void tri_backtransform(const cx<T>* A, cx<T>* W, int m, int k, int ld, SmallSmem<T>* sm) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int j = m - 2; j >= 0; --j) {
+    const cx<T> tau = sm->ttau[j];
+    if (tau.re == T(0) && tau.im == T(0)) continue;
+    const int L = m - j - 1;
+    // v^H W for each column: serial over rows, one thread per column (k <= 64)
+    for (int c = tid; c < k; c += nt) {
+      cx<T> acc = W[(j + 1) * ld + c];
+      for (int i = 1; i < L; ++i) fma_cj(acc, A[(j + 1 + i) * m + j], W[(j + 1 + i) * ld + c]);
+      sm->twv[c] = tau * acc;
+    }
+    __syncthreads();
+    for (int t = tid; t < L * k; t += nt) {
+      const int i = t / k, c = t - i * k;
+      const cx<T> v = i == 0 ? mk<T>(1, 0) : A[(j + 1 + i) * m + j];
+      W[(j + 1 + i) * ld + c] = W[(j + 1 + i) * ld + c] - v * sm->twv[c];
+    }
+    __syncthreads();
+  }
+}
+
+// Orthonormalise the columns of Wc (m x k, ld k).  Newton-Schulz steps
+// W <- W - 1/2 W (W^H W - I) remove FP32 rounding from the orthonormality
+// (each step squares the defect; W W^H is a projector only to that defect,
+// so steps repeat until max|W^H W - I| < 1e-4, at most four); vectors from a
+// near-degenerate cluster can be far from orthogonal, and then a Householder
+// QR of W (leading columns kept) replaces the steps.  U is workspace
+// (>= k*k + m*k entries).  Returns where the result lies.
+template <typename T>
+__device__ const cx<T>* orthonormalize(cx<T>* Wc, int m, int k, cx<T>* U, SmallSmem<T>* sm) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  cx<T>* E = U;
+  cx<T>* cur = Wc;
+  cx<T>* nxt = U + k * k;
+  for (int it = 0; it < 4; ++it) {
+    if (tid == 0) sm->ival[5] = 0;
+    __syncthreads();
+    float emax_local = 0.f;
+    for (int t = tid; t < k * k; t += nt) {
+      const int a = t / k, b = t - a * k;
+      cx<T> acc = mk<T>(0, 0);
+      for (int i = 0; i < m; ++i) fma_cj(acc, cur[i * k + a], cur[i * k + b]);
+      if (a == b) acc.re -= T(1);
+      E[t] = acc;
+      emax_local = fmaxf(emax_local, (float)sqrt(abs2(acc)));
+    }
+    atomicMax(&sm->ival[5], __float_as_int(emax_local));
+    __syncthreads();
+    const float emax = __int_as_float(sm->ival[5]);
+    if (it == 0 && emax > 0.05f) {
+      householder_qr<T>(Wc, m, k, U, sm);
+      return Wc;
+    }
+    for (int t = tid; t < m * k; t += nt) {
+      const int i = t / k, j = t - i * k;
+      cx<T> corr = mk<T>(0, 0);
+      for (int l = 0; l < k; ++l) fma_c(corr, cur[i * k + l], E[l * k + j]);
+      nxt[t] = cur[t] - scl(corr, T(0.5));
+    }
+    __syncthreads();
+    cx<T>* tmp = cur;
+    cur = nxt;
+    nxt = tmp;
+    if (emax < 1e-4f) break;
+  }
+  return cur;
+}
+
+// Packed upper Gram G = X X^H of the staged X (m x nn, row stride ld) in 4x4
+// register tiles; returns the trace (block-wide).
+template <typename T>
+__device__ double gram_staged(const cx<T>* Xs, int m, int nn, int ld, cx<T>* Gp, SmallSmem<T>* sm) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  double tr_part = 0.0;
+  const int nb = (m + 3) >> 2;
+  const int ntiles = nb * (nb + 1) / 2;
+  for (int tt = tid; tt < ntiles; tt += nt) {
+    int bi = 0, rem = tt;
+    while (rem >= nb - bi) {
+      rem -= nb - bi;
+      ++bi;
+    }
+    const int bj = bi + rem;
+    int ri[4], rj[4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+      ri[a] = min(4 * bi + a, m - 1) * ld;
+      rj[a] = min(4 * bj + a, m - 1) * ld;
+    }
+    cx<T> acc[4][4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int b = 0; b < 4; ++b) acc[a][b] = mk<T>(0, 0);
+    for (int c = 0; c < nn; ++c) {
+      cx<T> xi[4], xj[4];
+#pragma unroll
+      for (int a = 0; a < 4; ++a) {
+        xi[a] = Xs[ri[a] + c];
+        xj[a] = Xs[rj[a] + c];
+      }
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) fma_c(acc[a][b], xi[a], conj(xj[b]));
+    }
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int b = 0; b < 4; ++b) {
+        const int i = 4 * bi + a, j = 4 * bj + b;
+        if (i < m && j < m && i <= j) {
+          cx<T> v = acc[a][b];
+          if (i == j) {
+            v.im = T(0);
+            tr_part += (double)v.re;
+          }
+          Gp[pidx(i, j, m)] = v;
+        }
+      }
+  }
+  return block_sum(tr_part, sm->red);
+}
+
+// Eigenvalues of the packed Hermitian Gp (FP32 path): expanded into Af, reduced
+// to tridiagonal form (reflectors stay in Af), all eigenvalues by bisection
+// into sm->lam, and sm->perm ordering them descending.
+template <typename T>
+__device__ void eigvals_sorted(const cx<T>* Gp, cx<T>* Af, int m, double trace, SmallSmem<T>* sm) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int t = tid; t < m * m; t += nt) {
+    const int i = t / m, j = t - i * m;
+    Af[t] = gget(Gp, i, j, m);
+  }
+  __syncthreads();
+  tridiagonalize<T>(Af, m, trace, sm);
+  tri_bisect<T>(m, sm);
+  for (int i = tid; i < m; i += nt) {
+    const double li = sm->lam[i];
+    int rank = 0;
+    for (int j = 0; j < m; ++j) {
+      const double lj = sm->lam[j];
+      rank += (lj > li) || (lj == li && j < i);
+    }
+    sm->perm[rank] = i;
+  }
+  __syncthreads();
+}
+
+// Kept dimension for descending eigenvalues lam[0..mm) (squared singular
+// values): ExaTN's absolute per-index cutoff (truncateSvdTensors,
+// ExaTnMpsVisitor.cpp:2366-2536) or ITensor's relative truncate
+// (decomp.cc:307-463, mindim 1), both capped at chi.
+__device__ int decide_keep(const double* lam, int mm, const ProgDesc& P) {
+  int k = mm;
+  const int cap = P.chi_cap;
+  if (P.mode == TRUNC_EXATN) {
+    // first index whose partial norms (= singular value) are below the cutoff, keep it too
+    for (int i = 0; i < mm; ++i) {
+      const double v = lam[i];
+      const double sv = v > 0.0 ? sqrt(v) : 0.0;
+      if (sv < P.cutoff) {
+        k = i + 1;
+        break;
+      }
+    }
+    if (k > cap) k = cap;
+  } else {
+    const double p0 = lam[0];
+    if (!(p0 > 0.0) || mm == 1) {
+      k = 1;
+    } else {
+      double scale = 0.0;
+      for (int i = 0; i < mm; ++i) {
+        const double v = lam[i] / p0;
+        scale += v > 0.0 ? v : 0.0;
+      }
+      int n = mm - 1;
+      double err = 0.0;
+      while (n >= cap) {
+        const double v = lam[n] / p0;
+        err += v > 0.0 ? v : 0.0;
+        --n;
+      }
+      if (scale == 0.0) scale = 1.0;
+      while (n >= 1) {
+        const double v = lam[n] / p0;
+        const double pv = v > 0.0 ? v : 0.0;
+        if (err + pv > P.cutoff * scale) break;
+        err += pv;
+        --n;
+      }
+      k = n + 1;
+    }
+  }
+  return k < 1 ? 1 : k;
 }
 
 // ------------------------------------------------------------------- ops
@@ -389,7 +856,7 @@ __device__ void op_gate2(const ProgDesc& P, const DevOp& op, char* big, SmallSme
   cx<T>* U = Prec<T>::u_in_smem ? reinterpret_cast<cx<T>*>(big + Layout<T>::gram_bytes)
                                 : reinterpret_cast<cx<T>*>(scratch + sizeof(cx<T>) * kMaxM * kMaxM);
   const long long c_theta = clock64();
-  double tr_part = 0.0;
+  double trace;
   if (Prec<T>::u_in_smem) {
     // Stage X (m x nn) in the U region with a padded row stride, then form
     // the upper triangle of G = X X^H in 4x4 register tiles.
@@ -405,54 +872,9 @@ __device__ void op_gate2(const ProgDesc& P, const DevOp& op, char* big, SmallSme
       }
     }
     __syncthreads();
-    const int nb = (m + 3) >> 2;
-    const int ntiles = nb * (nb + 1) / 2;
-    for (int tt = tid; tt < ntiles; tt += nt) {
-      int bi = 0, rem = tt;
-      while (rem >= nb - bi) {
-        rem -= nb - bi;
-        ++bi;
-      }
-      const int bj = bi + rem;
-      int ri[4], rj[4];
-#pragma unroll
-      for (int a = 0; a < 4; ++a) {
-        ri[a] = min(4 * bi + a, m - 1) * ld;
-        rj[a] = min(4 * bj + a, m - 1) * ld;
-      }
-      cx<T> acc[4][4];
-#pragma unroll
-      for (int a = 0; a < 4; ++a)
-#pragma unroll
-        for (int b = 0; b < 4; ++b) acc[a][b] = mk<T>(0, 0);
-      for (int c = 0; c < nn; ++c) {
-        cx<T> xi[4], xj[4];
-#pragma unroll
-        for (int a = 0; a < 4; ++a) {
-          xi[a] = Xs[ri[a] + c];
-          xj[a] = Xs[rj[a] + c];
-        }
-#pragma unroll
-        for (int a = 0; a < 4; ++a)
-#pragma unroll
-          for (int b = 0; b < 4; ++b) fma_c(acc[a][b], xi[a], conj(xj[b]));
-      }
-#pragma unroll
-      for (int a = 0; a < 4; ++a)
-#pragma unroll
-        for (int b = 0; b < 4; ++b) {
-          const int i = 4 * bi + a, j = 4 * bj + b;
-          if (i < m && j < m && i <= j) {
-            cx<T> v = acc[a][b];
-            if (i == j) {
-              v.im = T(0);
-              tr_part += (double)v.re;
-            }
-            Gp[pidx(i, j, m)] = v;
-          }
-        }
-    }
+    trace = gram_staged<T>(Xs, m, nn, ld, Gp, sm);
   } else {
+    double tr_part = 0.0;
     for (int t = tid; t < m * m; t += nt) {
       const int i = t / m, j = t - i * m;
       if (i > j) continue;
@@ -464,79 +886,103 @@ __device__ void op_gate2(const ProgDesc& P, const DevOp& op, char* big, SmallSme
       }
       Gp[pidx(i, j, m)] = acc;
     }
+    trace = block_sum(tr_part, sm->red);
   }
-  const double trace = block_sum(tr_part, sm->red);
   const long long c_gram = clock64();
-  const int nrot_total = jacobi_eigh<T>(Gp, U, m, trace, sm);
-  const long long c_eig = clock64();
-  // eigenvalues, descending order
-  for (int i = tid; i < m; i += nt) sm->lam[i] = (double)Gp[pidx(i, i, m)].re;
-  __syncthreads();
-  for (int i = tid; i < m; i += nt) {
-    const double li = sm->lam[i];
-    int rank = 0;
-    for (int j = 0; j < m; ++j) {
-      const double lj = sm->lam[j];
-      rank += (lj > li) || (lj == li && j < i);
+  const int mm = R < Cc ? R : Cc;  // number of singular values (min(vol) in ExaTnMpsVisitor.cpp:1594)
+  int nrot_total = 0;
+  if (Prec<T>::u_in_smem) {
+    // FP32: reduce G (expanded into the U region) to tridiagonal form
+    eigvals_sorted<T>(Gp, U, m, trace, sm);
+  } else {
+    nrot_total = jacobi_eigh<T>(Gp, U, m, trace, sm);
+    // eigenvalues on the diagonal, ranked descending
+    for (int i = tid; i < m; i += nt) sm->lam[i] = (double)Gp[pidx(i, i, m)].re;
+    __syncthreads();
+    for (int i = tid; i < m; i += nt) {
+      const double li = sm->lam[i];
+      int rank = 0;
+      for (int j = 0; j < m; ++j) {
+        const double lj = sm->lam[j];
+        rank += (lj > li) || (lj == li && j < i);
+      }
+      sm->perm[rank] = i;
     }
-    sm->perm[rank] = i;
+    __syncthreads();
   }
+  for (int r = tid; r < m; r += nt) sm->lk[r] = sm->lam[sm->perm[r]];
   __syncthreads();
+  // FP32 small-eigenvalue refinement.  An FP32 Gram resolves eigenvalues only
+  // down to ~eps * trace, so when the cut falls among eigenvalues below
+  // kRefineRatio * lambda_max the kept subspace is re-chosen in the
+  // complement of the head (the eigenvectors above that ratio): Z = X -
+  // W_h (W_h^H X) has norm ~ the tail's, its own Gram resolves the tail to
+  // ~eps * |Z|^2, and the kept tail vectors are its leading eigenvectors.
+  // This is ITensor's recursive SVD refinement (SVDRefImpl, tensor/algs.cc:
+  // 510-579, checkSVDDone :486-507) in a deflated form, one level deep.
+  cx<T>* Wc = reinterpret_cast<cx<T>*>(big);
+  cx<T>* Wg = reinterpret_cast<cx<T>*>(scratch) + kMaxM * kMaxM;  // head vectors (m x s)
+  double refine_flops = 0.0;
+  if (Prec<T>::u_in_smem) {
+    if (tid == 0) {
+      const int k0 = decide_keep(sm->lk, mm, P);
+      const double l0 = sm->lk[0];
+      int s = 0;
+      while (s < m && sm->lk[s] >= kRefineRatio * l0) ++s;
+      sm->ival[6] = s;
+      sm->ival[7] = (l0 > 0.0 && s < k0 && k0 < m) ? 1 : 0;
+    }
+    __syncthreads();
+    const int s = sm->ival[6];
+    if (sm->ival[7]) {
+      for (int c = tid; c < s; c += nt) {
+        const int ev = sm->perm[c];
+        tri_twisted<T>(Wc, m, s, c, T(sm->lam[ev]), sm->bs[ev], sm->bt[ev], sm);
+      }
+      __syncthreads();
+      tri_backtransform<T>(U, Wc, m, s, s, sm);
+      const cx<T>* Wh = orthonormalize<T>(Wc, m, s, U, sm);
+      for (int t = tid; t < m * s; t += nt) Wg[t] = Wh[t];
+      __syncthreads();
+      // Y_h = W_h^H X (s x nn) in the Gram region
+      cx<T>* Yh = Gp;
+      for (int t = tid; t < s * nn; t += nt) {
+        const int j = t / nn, c = t - j * nn;
+        cx<T> acc = mk<T>(0, 0);
+        for (int i = 0; i < m; ++i) fma_cj(acc, Wg[i * s + j], X(i, c));
+        Yh[t] = acc;
+      }
+      __syncthreads();
+      // Z = X - W_h Y_h, staged like X
+      cx<T>* Zs = U;
+      const int ld = nn + 1;
+      for (int t = tid; t < m * nn; t += nt) {
+        const int i = t / nn, c = t - i * nn;
+        cx<T> acc = X(i, c);
+        for (int j = 0; j < s; ++j) acc = acc - Wg[i * s + j] * Yh[j * nn + c];
+        Zs[i * ld + c] = acc;
+      }
+      __syncthreads();
+      const double trz = gram_staged<T>(Zs, m, nn, ld, Gp, sm);
+      eigvals_sorted<T>(Gp, U, m, trz, sm);
+      for (int r = s + tid; r < m; r += nt) sm->lk[r] = sm->lam[sm->perm[r - s]];
+      __syncthreads();
+      refine_flops = 16.0 * m * s * nn + 8.0 * m * m * nn;
+    }
+  }
+  const long long c_eig = clock64();
   if (tid == 0) {
-    const int mm = R < Cc ? R : Cc;  // number of singular values (min(vol) in ExaTnMpsVisitor.cpp:1594)
     double total = 0.0;
     int bad = 0;
     for (int i = 0; i < mm; ++i) {
-      const double v = sm->lam[sm->perm[i]];
+      const double v = sm->lk[i];
       if (!(v == v) || isinf(v)) bad = 1;
       total += v > 0.0 ? v : 0.0;
     }
-    int k = mm;
-    const int cap = P.chi_cap;
-    if (P.mode == TRUNC_EXATN) {
-      // first index whose partial norms (= singular value) are below the cutoff, keep it too
-      for (int i = 0; i < mm; ++i) {
-        const double v = sm->lam[sm->perm[i]];
-        const double sv = v > 0.0 ? sqrt(v) : 0.0;
-        if (sv < P.cutoff) {
-          k = i + 1;
-          break;
-        }
-      }
-      if (k > cap) k = cap;
-    } else {
-      // ITensor truncate (decomp.cc:307-463), relative cutoff, mindim 1
-      const double p0 = sm->lam[sm->perm[0]];
-      if (!(p0 > 0.0) || mm == 1) {
-        k = 1;
-      } else {
-        double scale = 0.0;
-        for (int i = 0; i < mm; ++i) {
-          const double v = sm->lam[sm->perm[i]] / p0;
-          scale += v > 0.0 ? v : 0.0;
-        }
-        int n = mm - 1;
-        double err = 0.0;
-        while (n >= cap) {
-          const double v = sm->lam[sm->perm[n]] / p0;
-          err += v > 0.0 ? v : 0.0;
-          --n;
-        }
-        if (scale == 0.0) scale = 1.0;
-        while (n >= 1) {
-          const double v = sm->lam[sm->perm[n]] / p0;
-          const double pv = v > 0.0 ? v : 0.0;
-          if (err + pv > P.cutoff * scale) break;
-          err += pv;
-          --n;
-        }
-        k = n + 1;
-      }
-    }
-    if (k < 1) k = 1;
+    const int k = decide_keep(sm->lk, mm, P);
     double kept = 0.0;
     for (int i = 0; i < k; ++i) {
-      const double v = sm->lam[sm->perm[i]];
+      const double v = sm->lk[i];
       kept += v > 0.0 ? v : 0.0;
     }
     const double frac = total > 0.0 ? (total - kept) / total : 0.0;
@@ -549,16 +995,20 @@ __device__ void op_gate2(const ProgDesc& P, const DevOp& op, char* big, SmallSme
     P.stats[ST_N_GATE2] += 1.0;
     // algorithmic flops (complex MAC = 8): merge, gate, Gram, split
     P.stats[ST_FLOPS] += 32.0 * dl * dm * dr + 128.0 * dl * dr + 8.0 * m * m * nn + 8.0 * k * nn * m +
-                         (Prec<T>::u_in_smem ? 16.0 * m * k * k : 0.0);
+                         (Prec<T>::u_in_smem ? 16.0 * m * k * k : 0.0) + refine_flops +
+                         (Prec<T>::u_in_smem && k < m ? 16.0 * m * nn * k + 16.0 * m * k * k : 0.0);
     // each rotation updates two rows and two columns of G and two columns of U
-    P.stats[ST_EIG_FLOPS] += 96.0 * m * nrot_total;
+    P.stats[ST_EIG_FLOPS] += Prec<T>::u_in_smem ? (32.0 / 3.0) * m * m * m * (refine_flops > 0.0 ? 2.0 : 1.0) +
+                                                      8.0 * m * m * k
+                                                : 96.0 * m * nrot_total;
+    if (refine_flops > 0.0) P.stats[ST_N_REFINE] += 1.0;
     if (bad) atomicOr(P.err, ERR_NAN);
   }
   __syncthreads();
   const int k = sm->ival[2];
   const double rn = sm->dval[2];
   for (int j = tid; j < k; j += nt) {
-    const double v = sm->lam[sm->perm[j]];
+    const double v = sm->lk[j];
     const double sv = v > 0.0 ? sqrt(v) : 0.0;
     if (op.orient == ORIENT_SQRT) {
       const double h = sqrt(sv);
@@ -570,39 +1020,93 @@ __device__ void op_gate2(const ProgDesc& P, const DevOp& op, char* big, SmallSme
     }
   }
   __syncthreads();
-  // Kept eigenvectors W_k (m x k, ld k).  In FP32 the ~m*sweeps accumulated
-  // rotations leave the columns ~1e-5 off orthonormal, which would drift the
-  // norm by that much per gate; one Newton-Schulz step
-  // W <- W - 1/2 W (W^H W - I) restores orthonormality to FP32 rounding.
-  // The Gram region holds the compacted W, the U region E and the result.
+  // Kept eigenvectors W_k (m x k, ld k) in the Gram region.
   const cx<T>* W;
   if (Prec<T>::u_in_smem) {
-    cx<T>* Wc = reinterpret_cast<cx<T>*>(big);
-    for (int t = tid; t < m * k; t += nt) {
-      const int i = t / k, j = t - i * k;
-      Wc[t] = U[i * m + sm->perm[j]];
+    // FP32: twisted-factorisation vectors of the tridiagonal matrix,
+    // back-transformed by the reflectors still held in the U region; with the
+    // refinement, the head columns come from W_h and the rest from Z.
+    if (sm->ival[7]) {
+      const int s = sm->ival[6];
+      const int ks = k < s ? k : s, kt = k - ks;
+      for (int c = tid; c < kt; c += nt) {
+        const int ev = sm->perm[c];
+        tri_twisted<T>(Wc + ks, m, k, c, T(sm->lam[ev]), sm->bs[ev], sm->bt[ev], sm);
+      }
+      __syncthreads();
+      if (kt > 0) {
+        tri_backtransform<T>(U, Wc + ks, m, kt, k, sm);
+        // Gram-Schmidt the tail columns against the head (kt > 0 means ks == s):
+        // Z's rounding leaves components along W_h that a symmetric
+        // orthonormalisation would otherwise spread into the head.
+        cx<T>* Pr = U;  // W_h^H W_t (s x kt)
+        for (int t = tid; t < s * kt; t += nt) {
+          const int a = t / kt, c = t - a * kt;
+          cx<T> acc = mk<T>(0, 0);
+          for (int i = 0; i < m; ++i) fma_cj(acc, Wg[i * s + a], Wc[i * k + ks + c]);
+          Pr[t] = acc;
+        }
+        __syncthreads();
+        for (int t = tid; t < m * kt; t += nt) {
+          const int i = t / kt, c = t - i * kt;
+          cx<T> acc = Wc[i * k + ks + c];
+          for (int a = 0; a < s; ++a) acc = acc - Wg[i * s + a] * Pr[a * kt + c];
+          Wc[i * k + ks + c] = acc;
+        }
+        __syncthreads();
+      }
+      for (int t = tid; t < m * ks; t += nt) {
+        const int i = t / ks, j = t - i * ks;
+        Wc[i * k + j] = Wg[i * s + j];
+      }
+    } else {
+      for (int c = tid; c < k; c += nt) {
+        const int ev = sm->perm[c];
+        tri_twisted<T>(Wc, m, k, c, T(sm->lam[ev]), sm->bs[ev], sm->bt[ev], sm);
+      }
+      __syncthreads();
+      tri_backtransform<T>(U, Wc, m, k, k, sm);
     }
-    __syncthreads();
-    cx<T>* E = U;
-    cx<T>* Wn = U + k * k;
-    for (int t = tid; t < k * k; t += nt) {
-      const int a = t / k, b = t - a * k;
-      cx<T> acc = mk<T>(0, 0);
-      for (int i = 0; i < m; ++i) fma_cj(acc, Wc[i * k + a], Wc[i * k + b]);
-      if (a == b) acc.re -= T(1);
-      E[t] = acc;
+    W = orthonormalize<T>(Wc, m, k, U, sm);
+    if (k < m) {
+      // One subspace-iteration step W <- orth(X (X^H W)) with X itself, not
+      // the FP32 Gram: the Gram's rounding (~eps * trace) tilts a kept
+      // eigenvector into the discarded space by ~eps * trace / lambda, while
+      // the product's rounding is ~eps * sigma_max / sigma relative, so the
+      // weight lost to the cut drops from ~eps^2 trace^2 / lambda to
+      // ~eps^2 sigma_max^2 (the accuracy of a backward-stable SVD).
+      cx<T>* Wk = Wg;                     // W copied out (m x k)
+      cx<T>* Yv = Wg + kMaxM * kChiLimit;  // X^H W (nn x k)
+      for (int t = tid; t < m * k; t += nt) Wk[t] = W[t];
+      __syncthreads();
+      for (int t = tid; t < nn * k; t += nt) {
+        const int c = t / k, j = t - c * k;
+        cx<T> acc = mk<T>(0, 0);
+        for (int i = 0; i < m; ++i) fma_cj(acc, X(i, c), Wk[i * k + j]);
+        Yv[t] = acc;
+      }
+      __syncthreads();
+      for (int t = tid; t < m * k; t += nt) {
+        const int i = t / k, j = t - i * k;
+        cx<T> acc = mk<T>(0, 0);
+        for (int c = 0; c < nn; ++c) fma_c(acc, X(i, c), Yv[c * k + j]);
+        Wc[t] = acc;
+      }
+      __syncthreads();
+      for (int j = tid; j < k; j += nt) {
+        double s2 = 0.0;
+        for (int i = 0; i < m; ++i) s2 += (double)abs2(Wc[i * k + j]);
+        sm->lam[j] = s2;  // free after the eigenvector stage
+      }
+      __syncthreads();
+      for (int t = tid; t < m * k; t += nt) {
+        const int j = t - (t / k) * k;
+        const double s2 = sm->lam[j];
+        Wc[t] = s2 > 1e-60 ? scl(Wc[t], T(1.0 / sqrt(s2))) : Wk[t];
+      }
+      W = orthonormalize<T>(Wc, m, k, U, sm);
     }
-    __syncthreads();
-    for (int t = tid; t < m * k; t += nt) {
-      const int i = t / k, j = t - i * k;
-      cx<T> corr = mk<T>(0, 0);
-      for (int l = 0; l < k; ++l) fma_c(corr, Wc[i * k + l], E[l * k + j]);
-      Wn[t] = Wc[t] - scl(corr, T(0.5));
-    }
-    __syncthreads();
-    W = Wn;
   } else {
-    cx<T>* Wc = reinterpret_cast<cx<T>*>(big);
     for (int t = tid; t < m * k; t += nt) {
       const int i = t / k, j = t - i * k;
       Wc[t] = U[i * m + sm->perm[j]];

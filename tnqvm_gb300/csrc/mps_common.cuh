@@ -93,7 +93,8 @@ enum StatSlot {
   ST_CYC_EIG = 8,
   ST_CYC_SPLIT = 9,
   ST_CYC_MOVE = 10,
-  ST_COUNT = 11,
+  ST_N_REFINE = 11,   // two-site splits whose small-eigenvalue block was re-solved
+  ST_COUNT = 12,
 };
 
 // Error bits written by the kernels into ProgDesc::err.
