@@ -27,17 +27,26 @@ namespace gbmps {
 
 template <typename T>
 struct Prec;
+// u_in_smem: the m x m work matrix of the eigensolver (and the staged X)
+// fits next to the packed Gram in shared memory (FP32), else it lives in the
+// CTA's global scratch (FP64, L2-resident).  refine: the FP32-only accuracy
+// steps of the split.  bisect_rounds: 5-section rounds, each shrinking the
+// bracket 5x, to reach ~eps of the spectrum's span.
 template <>
 struct Prec<float> {
   static constexpr double eps = 1.1920929e-07;
   static constexpr bool u_in_smem = true;
-  static constexpr int max_sweeps = 24;
+  static constexpr bool refine = true;
+  static constexpr int bisect_rounds = 16;
+  static constexpr double ns_stop = 1e-4;  // last Newton-Schulz step leaves ~1.5 ns_stop^2 < eps
 };
 template <>
 struct Prec<double> {
   static constexpr double eps = 2.220446049250313e-16;
   static constexpr bool u_in_smem = false;
-  static constexpr int max_sweeps = 30;
+  static constexpr bool refine = false;
+  static constexpr int bisect_rounds = 26;
+  static constexpr double ns_stop = 1e-8;
 };
 
 __device__ __forceinline__ int pidx(int i, int j, int m) {  // i <= j
@@ -54,16 +63,6 @@ __device__ __forceinline__ void gset(cx<T>* Gp, int i, int j, int m, cx<T> v) {
     Gp[pidx(i, j, m)] = v;
   else
     Gp[pidx(j, i, m)] = conj(v);
-}
-
-__device__ __forceinline__ void rr_pair(int m, int r, int j, int& p, int& q) {
-  if (j == 0) {
-    p = m - 1;
-    q = r;
-  } else {
-    p = (r + j) % (m - 1);
-    q = (r - j + m - 1) % (m - 1);
-  }
 }
 
 // Block-wide sum of a double; `red` holds >= 32 doubles of shared memory.
@@ -87,14 +86,9 @@ struct SmallSmem {
   int perm[kMaxM];
   T iso[kMaxM];
   T oth[kMaxM];
-  int rp_p[kMaxM / 2], rp_q[kMaxM / 2];  // pairs of the current Jacobi step
-  int pos[kMaxM / 2];                    // slot of an active pair, -1 if it does not rotate
-  int sp[kMaxM / 2], sq[kMaxM / 2];      // per slot: the pair, its rotation c, s, e
-  T sc[kMaxM / 2], ss[kMaxM / 2];
-  cx<T> se[kMaxM / 2];
   cx<T> g[16];
   cx<T> tau[kChiLimit];
-  // tridiagonal eigensolver (FP32 path)
+  // tridiagonal eigensolver
   cx<T> ttau[kMaxM];     // Householder scalars of the tridiagonalisation
   cx<T> tv[kMaxM];       // current reflector v
   cx<T> tp[kMaxM];       // p = tau A v, then w
@@ -116,8 +110,9 @@ struct Layout {
   static constexpr size_t qr_bytes = sizeof(cx<T>) * (kMaxM * kChiLimit + kChiLimit * kChiLimit);
   static constexpr size_t big = (gram_bytes + u_bytes) > qr_bytes ? (gram_bytes + u_bytes) : qr_bytes;
   static constexpr size_t smem = big + sizeof(SmallSmem<T>);
-  // Global scratch per CTA: theta, then U for FP64, or for FP32 two m x chi
-  // blocks (the refinement's head vectors, then the subspace step's X^H W).
+  // Global scratch per CTA: theta, then the eigensolver's work matrix for
+  // FP64, or for FP32 two m x chi blocks (the refinement's head vectors, then
+  // the subspace step's X^H W).
   static constexpr size_t scratch =
       sizeof(cx<T>) * (kMaxM * kMaxM + (Prec<T>::u_in_smem ? 2 * kMaxM * kChiLimit : kMaxM * kMaxM));
 };
@@ -126,127 +121,6 @@ struct Layout {
 // form the tail that is re-solved (singular-value ratio 1e-2; the FP32 Gram's
 // absolute error is ~1e-7 of the trace).
 constexpr double kRefineRatio = 1e-4;
-
-// ------------------------------------------------------------------ Jacobi
-// Diagonalise the m x m Hermitian matrix held packed in Gp; U (ld = m)
-// receives the eigenvectors as columns; eigenvalues are left on the diagonal.
-template <typename T>
-__device__ int jacobi_eigh(cx<T>* Gp, cx<T>* U, int m, double trace, SmallSmem<T>* sm) {
-  const int tid = threadIdx.x, nt = blockDim.x;
-  int total_rot = 0;
-  for (int t = tid; t < m * m; t += nt) {
-    const int i = t / m, j = t - i * m;
-    U[t] = mk<T>(i == j ? T(1) : T(0), T(0));
-  }
-  __syncthreads();
-  const int np = m >> 1;
-  const T tol_rel = T(Prec<T>::eps);
-  // Relative threshold only, with a floor far below FP rounding of the trace: an
-  // absolute eps*trace floor leaves off-diagonals that mix kept and discarded
-  // eigenvectors across small gaps and costs accuracy after truncation.
-  const T tol_abs = T(64.0 * Prec<T>::eps * Prec<T>::eps * trace);
-  // Two per-step counters of active rotations, alternating with a global step
-  // index: the counter of step s+1 is cleared during step s's rotation phase,
-  // which every thread reaches only after all have read the count of step s-1
-  // (or that count was zero, in which case clearing it changes nothing).
-  if (tid == 0) {
-    sm->ival[3] = 0;
-    sm->ival[4] = 0;
-  }
-  __syncthreads();
-  int gs = 0;
-  for (int sweep = 0; sweep < Prec<T>::max_sweeps; ++sweep) {
-    int nrot = 0;
-    for (int r = 0; r < m - 1; ++r, ++gs) {
-      int* cnt = &sm->ival[3 + (gs & 1)];
-      if (tid == 0) sm->ival[3 + ((gs + 1) & 1)] = 0;
-      // Rotation of each pair j: J = [[c, s], [-s e*, c e*]] with e = g/|g|,
-      // listed compactly by slot for the update phase.
-      for (int j = tid; j < np; j += nt) {
-        int p, q;
-        rr_pair(m, r, j, p, q);
-        const T a = Gp[pidx(p, p, m)].re, b = Gp[pidx(q, q, m)].re;
-        const cx<T> g = gget(Gp, p, q, m);
-        const T ag = sqrt(abs2(g));
-        sm->rp_p[j] = p;
-        sm->rp_q[j] = q;
-        if (ag > tol_abs && ag > tol_rel * sqrt(fabs(a * b))) {
-          const T zeta = (b - a) / (T(2) * ag);
-          const T tt = (zeta >= T(0) ? T(1) : T(-1)) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
-          const T c = T(1) / sqrt(T(1) + tt * tt);
-          const int slot = atomicAdd(cnt, 1);
-          sm->pos[j] = slot;
-          sm->sp[slot] = p;
-          sm->sq[slot] = q;
-          sm->sc[slot] = c;
-          sm->ss[slot] = c * tt;
-          sm->se[slot] = mk<T>(g.re / ag, g.im / ag);
-        } else {
-          sm->pos[j] = -1;
-        }
-      }
-      __syncthreads();
-      const int na = *cnt;
-      nrot += na;
-      if (na == 0) continue;  // nothing rotates: G and U unchanged, no second barrier needed
-      // G <- J^H G J as independent 2x2 block updates over the pair blocks
-      // that touch an active rotation; a block of two active pairs is done
-      // once, by the one in the lower slot.
-      for (int t = tid; t < na * np; t += nt) {
-        const int ai = t / np, J = t - ai * np;
-        const int bj = sm->pos[J];
-        if (bj >= 0 && bj < ai) continue;
-        const int pI = sm->sp[ai], qI = sm->sq[ai];
-        const T cI = sm->sc[ai], sI = sm->ss[ai];
-        const cx<T> eI = sm->se[ai];
-        if (bj == ai) {  // diagonal block: the rotation zeroes G[p][q]
-          const T a = Gp[pidx(pI, pI, m)].re, b = Gp[pidx(qI, qI, m)].re;
-          const cx<T> g = gget(Gp, pI, qI, m);
-          // diag(J^H B J) with |g| = Re(g e*): a' = a - 2cs|g| ... written out
-          const T gr = g.re * eI.re + g.im * eI.im;
-          const T an = cI * cI * a + sI * sI * b - T(2) * cI * sI * gr;
-          const T bn = sI * sI * a + cI * cI * b + T(2) * cI * sI * gr;
-          Gp[pidx(pI, pI, m)] = mk<T>(an, 0);
-          Gp[pidx(qI, qI, m)] = mk<T>(bn, 0);
-          gset(Gp, pI, qI, m, mk<T>(0, 0));
-          continue;
-        }
-        const int pJ = sm->rp_p[J], qJ = sm->rp_q[J];
-        const cx<T> b00 = gget(Gp, pI, pJ, m), b01 = gget(Gp, pI, qJ, m);
-        const cx<T> b10 = gget(Gp, qI, pJ, m), b11 = gget(Gp, qI, qJ, m);
-        cx<T> c00 = b00, c01 = b01, c10 = b10, c11 = b11;
-        if (bj >= 0) {  // C = B J
-          const T cJ = sm->sc[bj], sJ = sm->ss[bj];
-          const cx<T> eJc = conj(sm->se[bj]);
-          const cx<T> u0 = b01 * eJc, u1 = b11 * eJc;
-          c00 = scl(b00, cJ) - scl(u0, sJ);
-          c01 = scl(b00, sJ) + scl(u0, cJ);
-          c10 = scl(b10, cJ) - scl(u1, sJ);
-          c11 = scl(b10, sJ) + scl(u1, cJ);
-        }
-        // D = J^H C, J^H = [[c, -s e], [s, c e]]
-        const cx<T> v0 = eI * c10, v1 = eI * c11;
-        gset(Gp, pI, pJ, m, scl(c00, cI) - scl(v0, sI));
-        gset(Gp, pI, qJ, m, scl(c01, cI) - scl(v1, sI));
-        gset(Gp, qI, pJ, m, scl(c00, sI) + scl(v0, cI));
-        gset(Gp, qI, qJ, m, scl(c01, sI) + scl(v1, cI));
-      }
-      // U <- U J on the columns of the active pairs
-      for (int t = tid; t < m * na; t += nt) {
-        const int row = t / na, a = t - row * na;
-        const int p = sm->sp[a], q = sm->sq[a];
-        const T c = sm->sc[a], s = sm->ss[a];
-        const cx<T> up = U[row * m + p], uqe = U[row * m + q] * conj(sm->se[a]);
-        U[row * m + p] = scl(up, c) - scl(uqe, s);
-        U[row * m + q] = scl(up, s) + scl(uqe, c);
-      }
-      __syncthreads();
-    }
-    total_rot += nrot;
-    if (nrot == 0) break;
-  }
-  return total_rot;
-}
 
 // ---------------------------------------------------------- Householder QR
 // M (mr x nc, ld = nc) -> Q in the first k = min(mr,nc) columns of M,
@@ -439,7 +313,7 @@ __device__ void tridiagonalize(cx<T>* A, int m, double trace, SmallSmem<T>* sm) 
 
 // All eigenvalues of T (td, te): split into unreduced blocks, then each row j
 // finds the (j - block start)-th smallest eigenvalue of its block with four
-// lanes multisecting the interval (16 rounds of 5-section, fixed count).
+// lanes multisecting the interval (a fixed number of 5-section rounds).
 // Results: sm->lam[j] and the block bounds sm->bs[j], sm->bt[j].
 template <typename T>
 __device__ void tri_bisect(int m, SmallSmem<T>* sm) {
@@ -487,7 +361,7 @@ __device__ void tri_bisect(int m, SmallSmem<T>* sm) {
   const T pad = T(4) * eps * fmax(fabs(lo), fabs(hi)) + pivmin;
   T a = lo - pad, b = hi + pad;
   const unsigned gmask = 0xFu << (threadIdx.x & 28);
-  for (int round = 0; round < 16; ++round) {
+  for (int round = 0; round < Prec<T>::bisect_rounds; ++round) {
     const T w = (b - a) / T(5);
     const T x = a + w * T(q + 1);
     int cnt = 0;
@@ -610,11 +484,12 @@ __device__ void tri_backtransform(const cx<T>* A, cx<T>* W, int m, int k, int ld
 }
 
 // Orthonormalise the columns of Wc (m x k, ld k).  Newton-Schulz steps
-// W <- W - 1/2 W (W^H W - I) remove FP32 rounding from the orthonormality
-// (each step squares the defect; W W^H is a projector only to that defect,
-// so steps repeat until max|W^H W - I| < 1e-4, at most four); vectors from a
-// near-degenerate cluster can be far from orthogonal, and then a Householder
-// QR of W (leading columns kept) replaces the steps.  U is workspace
+// W <- W - 1/2 W (W^H W - I) remove rounding from the orthonormality (each
+// step squares the defect; W W^H is a projector only to that defect, so steps
+// repeat until the step taken from |W^H W - I|_F < ns_stop leaves ~eps, at
+// most five); vectors from a near-degenerate cluster can be far from
+// orthogonal (|W^H W - I|_F > 0.1), and then a Householder QR of W (leading
+// columns kept) replaces the steps.  U is workspace
 // (>= k*k + m*k entries).  Returns where the result lies.
 template <typename T>
 __device__ const cx<T>* orthonormalize(cx<T>* Wc, int m, int k, cx<T>* U, SmallSmem<T>* sm) {
@@ -622,22 +497,20 @@ __device__ const cx<T>* orthonormalize(cx<T>* Wc, int m, int k, cx<T>* U, SmallS
   cx<T>* E = U;
   cx<T>* cur = Wc;
   cx<T>* nxt = U + k * k;
-  for (int it = 0; it < 4; ++it) {
-    if (tid == 0) sm->ival[5] = 0;
+  for (int it = 0; it < 5; ++it) {
     __syncthreads();
-    float emax_local = 0.f;
+    double f2 = 0.0;
     for (int t = tid; t < k * k; t += nt) {
       const int a = t / k, b = t - a * k;
       cx<T> acc = mk<T>(0, 0);
       for (int i = 0; i < m; ++i) fma_cj(acc, cur[i * k + a], cur[i * k + b]);
       if (a == b) acc.re -= T(1);
       E[t] = acc;
-      emax_local = fmaxf(emax_local, (float)sqrt(abs2(acc)));
+      f2 += (double)abs2(acc);
     }
-    atomicMax(&sm->ival[5], __float_as_int(emax_local));
-    __syncthreads();
-    const float emax = __int_as_float(sm->ival[5]);
-    if (it == 0 && emax > 0.05f) {
+    // |E|_2 <= |E|_F: below 0.1 the steps converge quadratically
+    const double fro = sqrt(block_sum(f2, sm->red));
+    if (it == 0 && fro > 0.1) {
       householder_qr<T>(Wc, m, k, U, sm);
       return Wc;
     }
@@ -651,7 +524,7 @@ __device__ const cx<T>* orthonormalize(cx<T>* Wc, int m, int k, cx<T>* U, SmallS
     cx<T>* tmp = cur;
     cur = nxt;
     nxt = tmp;
-    if (emax < 1e-4f) break;
+    if (fro < Prec<T>::ns_stop) break;
   }
   return cur;
 }
@@ -890,26 +763,8 @@ __device__ void op_gate2(const ProgDesc& P, const DevOp& op, char* big, SmallSme
   }
   const long long c_gram = clock64();
   const int mm = R < Cc ? R : Cc;  // number of singular values (min(vol) in ExaTnMpsVisitor.cpp:1594)
-  int nrot_total = 0;
-  if (Prec<T>::u_in_smem) {
-    // FP32: reduce G (expanded into the U region) to tridiagonal form
-    eigvals_sorted<T>(Gp, U, m, trace, sm);
-  } else {
-    nrot_total = jacobi_eigh<T>(Gp, U, m, trace, sm);
-    // eigenvalues on the diagonal, ranked descending
-    for (int i = tid; i < m; i += nt) sm->lam[i] = (double)Gp[pidx(i, i, m)].re;
-    __syncthreads();
-    for (int i = tid; i < m; i += nt) {
-      const double li = sm->lam[i];
-      int rank = 0;
-      for (int j = 0; j < m; ++j) {
-        const double lj = sm->lam[j];
-        rank += (lj > li) || (lj == li && j < i);
-      }
-      sm->perm[rank] = i;
-    }
-    __syncthreads();
-  }
+  // reduce G (expanded into the U work matrix) to tridiagonal form
+  eigvals_sorted<T>(Gp, U, m, trace, sm);
   for (int r = tid; r < m; r += nt) sm->lk[r] = sm->lam[sm->perm[r]];
   __syncthreads();
   // FP32 small-eigenvalue refinement.  An FP32 Gram resolves eigenvalues only
@@ -923,7 +778,7 @@ __device__ void op_gate2(const ProgDesc& P, const DevOp& op, char* big, SmallSme
   cx<T>* Wc = reinterpret_cast<cx<T>*>(big);
   cx<T>* Wg = reinterpret_cast<cx<T>*>(scratch) + kMaxM * kMaxM;  // head vectors (m x s)
   double refine_flops = 0.0;
-  if (Prec<T>::u_in_smem) {
+  if (Prec<T>::refine) {
     if (tid == 0) {
       const int k0 = decide_keep(sm->lk, mm, P);
       const double l0 = sm->lk[0];
@@ -995,12 +850,10 @@ __device__ void op_gate2(const ProgDesc& P, const DevOp& op, char* big, SmallSme
     P.stats[ST_N_GATE2] += 1.0;
     // algorithmic flops (complex MAC = 8): merge, gate, Gram, split
     P.stats[ST_FLOPS] += 32.0 * dl * dm * dr + 128.0 * dl * dr + 8.0 * m * m * nn + 8.0 * k * nn * m +
-                         (Prec<T>::u_in_smem ? 16.0 * m * k * k : 0.0) + refine_flops +
-                         (Prec<T>::u_in_smem && k < m ? 16.0 * m * nn * k + 16.0 * m * k * k : 0.0);
-    // each rotation updates two rows and two columns of G and two columns of U
-    P.stats[ST_EIG_FLOPS] += Prec<T>::u_in_smem ? (32.0 / 3.0) * m * m * m * (refine_flops > 0.0 ? 2.0 : 1.0) +
-                                                      8.0 * m * m * k
-                                                : 96.0 * m * nrot_total;
+                         16.0 * m * k * k + refine_flops +
+                         (Prec<T>::refine && k < m ? 16.0 * m * nn * k + 16.0 * m * k * k : 0.0);
+    // Householder tridiagonalisation (complex, both sides) and the back-transform
+    P.stats[ST_EIG_FLOPS] += (32.0 / 3.0) * m * m * m * (refine_flops > 0.0 ? 2.0 : 1.0) + 8.0 * m * m * k;
     if (refine_flops > 0.0) P.stats[ST_N_REFINE] += 1.0;
     if (bad) atomicOr(P.err, ERR_NAN);
   }
@@ -1022,11 +875,11 @@ __device__ void op_gate2(const ProgDesc& P, const DevOp& op, char* big, SmallSme
   __syncthreads();
   // Kept eigenvectors W_k (m x k, ld k) in the Gram region.
   const cx<T>* W;
-  if (Prec<T>::u_in_smem) {
-    // FP32: twisted-factorisation vectors of the tridiagonal matrix,
-    // back-transformed by the reflectors still held in the U region; with the
-    // refinement, the head columns come from W_h and the rest from Z.
-    if (sm->ival[7]) {
+  {
+    // twisted-factorisation vectors of the tridiagonal matrix, back-transformed
+    // by the reflectors still held in the U work matrix; with the refinement,
+    // the head columns come from W_h and the rest from Z.
+    if (Prec<T>::refine && sm->ival[7]) {
       const int s = sm->ival[6];
       const int ks = k < s ? k : s, kt = k - ks;
       for (int c = tid; c < kt; c += nt) {
@@ -1068,7 +921,7 @@ __device__ void op_gate2(const ProgDesc& P, const DevOp& op, char* big, SmallSme
       tri_backtransform<T>(U, Wc, m, k, k, sm);
     }
     W = orthonormalize<T>(Wc, m, k, U, sm);
-    if (k < m) {
+    if (Prec<T>::refine && k < m) {
       // One subspace-iteration step W <- orth(X (X^H W)) with X itself, not
       // the FP32 Gram: the Gram's rounding (~eps * trace) tilts a kept
       // eigenvector into the discarded space by ~eps * trace / lambda, while
@@ -1106,13 +959,6 @@ __device__ void op_gate2(const ProgDesc& P, const DevOp& op, char* big, SmallSme
       }
       W = orthonormalize<T>(Wc, m, k, U, sm);
     }
-  } else {
-    for (int t = tid; t < m * k; t += nt) {
-      const int i = t / k, j = t - i * k;
-      Wc[t] = U[i * m + sm->perm[j]];
-    }
-    __syncthreads();
-    W = Wc;
   }
   // other side: Z = W_k^H X (k x nn)
   for (int t = tid; t < k * nn; t += nt) {
@@ -1246,9 +1092,9 @@ k_run_ops(const ProgDesc* __restrict__ progs, int n_progs, int* queue, char* scr
   int pi = blockIdx.x;
   while (true) {
     if (queue != nullptr) {
-      if (threadIdx.x == 0) sm->ival[7] = atomicAdd(queue, 1);
+      if (threadIdx.x == 0) sm->ival[0] = atomicAdd(queue, 1);
       __syncthreads();
-      pi = sm->ival[7];
+      pi = sm->ival[0];
       __syncthreads();
     }
     if (pi >= n_progs) break;
