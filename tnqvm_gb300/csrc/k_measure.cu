@@ -18,63 +18,146 @@
 namespace gbmps {
 
 
+// Expectation sweep layout.  FP32 stages the site tensor, the partial
+// product X and the environment E in shared memory (160 KiB, one CTA per SM);
+// FP64 keeps E in shared memory and reads A and X through L1/L2.
 template <typename T>
-__device__ __forceinline__ cx<T> pauli_apply(const cx<T>* A, int dr, int l, int s, int r, int code) {
-  // (P A)[l][s][r] = sum_t P[s][t] A[l][t][r]
-  switch (code) {
-    case 1:
-      return A[(l * 2 + (1 - s)) * dr + r];
-    case 2: {
-      const cx<T> v = A[(l * 2 + (1 - s)) * dr + r];
-      // Y = [[0,-i],[i,0]]: s=0 -> -i A1, s=1 -> i A0
-      return s == 0 ? mk<T>(v.im, -v.re) : mk<T>(-v.im, v.re);
-    }
-    case 3: {
-      const cx<T> v = A[(l * 2 + s) * dr + r];
-      return s == 0 ? v : mk<T>(-v.re, -v.im);
-    }
-    default:
-      return A[(l * 2 + s) * dr + r];
-  }
-}
+struct ExpLayout {
+  static constexpr bool staged = sizeof(T) == 4;
+  static constexpr size_t a_elems = (size_t)kChiLimit * 2 * kChiLimit;  // A or X: (l, s, r)
+  static constexpr size_t e_elems = (size_t)kChiLimit * kChiLimit;
+  static constexpr size_t smem = sizeof(cx<T>) * (e_elems + (staged ? 2 * a_elems : 0));
+  static constexpr size_t scratch = staged ? 16 : sizeof(cx<T>) * a_elems;  // X per CTA (FP64)
+};
 
+// One CTA per (program, Pauli term): E <- sum_{l,s} A[l,s,:]^H (E P_s A)[l,s,:]
+// site by site.  Step 1 forms Y = E A (dl x 2dr) in 4(l) x 4(r) x 2(s)
+// register tiles and applies the site's Pauli as the 2x2 mix X[l,s,r] =
+// sum_s' P[s,s'] Y[l,s',r] in registers; step 2 forms E' = A_mat^H X
+// (A_mat = A as a (2dl) x dr matrix) in 4 x 4 tiles.
 template <typename T>
 __global__ void __launch_bounds__(256) k_expect(const ExpTask* __restrict__ tasks, int n_tasks, char* scratch,
                                                 size_t stride, double* out) {
+  using L = ExpLayout<T>;
   extern __shared__ __align__(16) char smem[];
-  cx<T>* E = reinterpret_cast<cx<T>*>(smem);
-  cx<T>* E2 = E + kChiLimit * kChiLimit;
+  cx<T>* E = reinterpret_cast<cx<T>*>(smem);  // ld kChiLimit
+  cx<T>* As = E + L::e_elems;                  // staged A (FP32)
+  cx<T>* X = L::staged ? As + L::a_elems : reinterpret_cast<cx<T>*>(scratch + stride * blockIdx.x);
   const int task = blockIdx.x;
   if (task >= n_tasks) return;
   const ExpTask tk = tasks[task];
-  cx<T>* X = reinterpret_cast<cx<T>*>(scratch + stride * blockIdx.x);
   const int tid = threadIdx.x, nt = blockDim.x;
+  constexpr int LD = kChiLimit;
   if (tid == 0) E[0] = mk<T>(1, 0);
-  __syncthreads();
   const cx<T>* sites = reinterpret_cast<const cx<T>*>(tk.sites);
   for (int i = 0; i < tk.n; ++i) {
     const int dl = tk.bond[i], dr = tk.bond[i + 1];
-    const cx<T>* A = sites + tk.site_off[i];
+    const cx<T>* Ag = sites + tk.site_off[i];
     const int code = tk.codes[i];
-    // X[(l,s)][r] = sum_l' E[l][l'] (P A)[l'][s][r]
-    for (int t = tid; t < dl * 2 * dr; t += nt) {
-      const int l = t / (2 * dr), rest = t - l * 2 * dr, s = rest / dr, r = rest - s * dr;
-      cx<T> acc = mk<T>(0, 0);
-      for (int lp = 0; lp < dl; ++lp) fma_c(acc, E[l * dl + lp], pauli_apply(A, dr, lp, s, r, code));
-      X[t] = acc;
+    const cx<T>* A;
+    if (L::staged) {
+      for (int t = tid; t < dl * 2 * dr; t += nt) As[t] = Ag[t];
+      A = As;
+    } else {
+      A = Ag;
     }
     __syncthreads();
-    // E'[r][r'] = sum_{l,s} conj(A[l][s][r]) X[(l,s)][r']
-    for (int t = tid; t < dr * dr; t += nt) {
-      const int r = t / dr, rp = t - r * dr;
-      cx<T> acc = mk<T>(0, 0);
-      for (int x = 0; x < 2 * dl; ++x) fma_cj(acc, A[x * dr + r], X[x * dr + rp]);
-      E2[t] = acc;
+    // step 1: X = P (E A), tiles of 4 rows l x 4 columns r x both s
+    {
+      const int nbl = (dl + 3) >> 2, nbr = (dr + 3) >> 2;
+      for (int tt = tid; tt < nbl * nbr; tt += nt) {
+        const int bl = tt / nbr, br = tt - bl * nbr;
+        int el[4], ar[4];
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+          el[a] = min(4 * bl + a, dl - 1) * LD;
+          ar[a] = min(4 * br + a, dr - 1);
+        }
+        cx<T> y0[4][4], y1[4][4];
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+          for (int b = 0; b < 4; ++b) y0[a][b] = y1[a][b] = mk<T>(0, 0);
+        for (int lp = 0; lp < dl; ++lp) {
+          cx<T> e[4], a0[4], a1[4];
+          const cx<T>* row0 = A + (lp * 2) * dr;
+          const cx<T>* row1 = row0 + dr;
+#pragma unroll
+          for (int a = 0; a < 4; ++a) {
+            e[a] = E[el[a] + lp];
+            a0[a] = row0[ar[a]];
+            a1[a] = row1[ar[a]];
+          }
+#pragma unroll
+          for (int a = 0; a < 4; ++a)
+#pragma unroll
+            for (int b = 0; b < 4; ++b) {
+              fma_c(y0[a][b], e[a], a0[b]);
+              fma_c(y1[a][b], e[a], a1[b]);
+            }
+        }
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+          for (int b = 0; b < 4; ++b) {
+            const int l = 4 * bl + a, r = 4 * br + b;
+            if (l < dl && r < dr) {
+              cx<T> x0 = y0[a][b], x1 = y1[a][b];
+              if (code == 1) {  // X
+                x0 = y1[a][b];
+                x1 = y0[a][b];
+              } else if (code == 2) {  // Y = [[0,-i],[i,0]]
+                x0 = mk<T>(y1[a][b].im, -y1[a][b].re);
+                x1 = mk<T>(-y0[a][b].im, y0[a][b].re);
+              } else if (code == 3) {  // Z
+                x1 = mk<T>(-x1.re, -x1.im);
+              }
+              X[(l * 2) * dr + r] = x0;
+              X[(l * 2 + 1) * dr + r] = x1;
+            }
+          }
+      }
     }
     __syncthreads();
-    cx<T>* tmp = E;
-    E = E2;
-    E2 = tmp;
+    // step 2: E'[r][r'] = sum_x conj(A[x][r]) X[x][r'], x = (l, s)
+    {
+      const int nb = (dr + 3) >> 2;
+      const int K = 2 * dl;
+      for (int tt = tid; tt < nb * nb; tt += nt) {
+        const int bi = tt / nb, bj = tt - bi * nb;
+        int ri[4], rj[4];
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+          ri[a] = min(4 * bi + a, dr - 1);
+          rj[a] = min(4 * bj + a, dr - 1);
+        }
+        cx<T> acc[4][4];
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+          for (int b = 0; b < 4; ++b) acc[a][b] = mk<T>(0, 0);
+        for (int x = 0; x < K; ++x) {
+          cx<T> av[4], xv[4];
+#pragma unroll
+          for (int a = 0; a < 4; ++a) {
+            av[a] = A[x * dr + ri[a]];
+            xv[a] = X[x * dr + rj[a]];
+          }
+#pragma unroll
+          for (int a = 0; a < 4; ++a)
+#pragma unroll
+            for (int b = 0; b < 4; ++b) fma_cj(acc[a][b], av[a], xv[b]);
+        }
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+          for (int b = 0; b < 4; ++b) {
+            const int r = 4 * bi + a, rp = 4 * bj + b;
+            if (r < dr && rp < dr) E[r * LD + rp] = acc[a][b];
+          }
+      }
+    }
+    __syncthreads();
   }
   if (tid == 0) {
     out[2 * task] = (double)E[0].re;
@@ -237,12 +320,8 @@ __global__ void __launch_bounds__(256) k_amp_one(const void* sites_v, const int6
 }
 
 // ------------------------------------------------------------- launchers
-size_t expect_smem_bytes(int prec) {
-  return (prec == 0 ? sizeof(cx<double>) : sizeof(cx<float>)) * 2 * kChiLimit * kChiLimit;
-}
-size_t expect_scratch_bytes(int prec) {
-  return (prec == 0 ? sizeof(cx<double>) : sizeof(cx<float>)) * 2 * kChiLimit * kChiLimit;
-}
+size_t expect_smem_bytes(int prec) { return prec == 0 ? ExpLayout<double>::smem : ExpLayout<float>::smem; }
+size_t expect_scratch_bytes(int prec) { return prec == 0 ? ExpLayout<double>::scratch : ExpLayout<float>::scratch; }
 
 template <typename T>
 static cudaError_t launch_expect_t(const ExpTask* d_tasks, int n_tasks, char* scratch, double* d_out,
