@@ -220,6 +220,11 @@ def run_ours(args):
     cycles = g.phase_cycles()
     cyc_total = sum(cycles.values()) or 1.0
     phase_share = {k: v / cyc_total for k, v in cycles.items()}
+    sums = g.stat_sums()
+    phase_share["eigensolver_detail"] = {k: sums["cyc_" + k] / cyc_total for k in ("trid", "bisect", "vec")}
+    phase_share["orthonormalise_in_split"] = sums["cyc_orth"] / cyc_total
+    phase_share["refined_splits"] = int(sums["refined"])
+    phase_share["splits"] = int(sums["gate2"])
     if dist is not None:
         t = torch.tensor([ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)

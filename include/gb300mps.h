@@ -163,6 +163,15 @@ int mps_graph_timing(mps_graph* g, double out[6]);
  * the fused update: out[0] theta, out[1] Gram, out[2] eigensolver, out[3]
  * truncation + split, out[4] centre moves. */
 int mps_graph_phase_cycles(mps_graph* g, double out[5]);
+/* Per-program statistics of the last replay summed over the graph's programs,
+ * slots 0..n-1 (n <= 16): 0 sum log(1 - discarded fraction), 1 largest
+ * discarded fraction (summed), 2 two-site splits, 3 ops, 4 GEMM-class flops,
+ * 5 eigensolver flops, 6-10 the phase cycles of mps_graph_phase_cycles, 11
+ * splits whose small-eigenvalue block was re-solved, 12-14 eigensolver cycles
+ * in tridiagonalisation, bisection and eigenvector formation, 15 cycles of
+ * orthonormalisation and the subspace step.  Diagnostics of this engine; no
+ * counterpart in the reference. */
+int mps_graph_stat_sums(mps_graph* g, double* out, int n);
 int mps_graph_destroy(mps_graph* g);
 
 /* Continuous-batching request loop (serving).  Requests are programs that

@@ -266,6 +266,20 @@ int mps_graph_phase_cycles(mps_graph* g, double out[5]) {
   return MPS_OK;
 }
 
+int mps_graph_stat_sums(mps_graph* g, double* out, int n) {
+  if (!g || !out) return fail(MPS_ERR_ARG, "NULL argument");
+  if (n < 1 || n > ST_COUNT) return fail(MPS_ERR_ARG, "n must be in 1..16");
+  GCK(cudaSetDevice(g->c->device));
+  GCK(cudaStreamSynchronize(g->L.stream));
+  for (int i = 0; i < n; ++i) out[i] = 0.0;
+  for (mps_prog* p : g->progs) {
+    double st[ST_COUNT];
+    GCK(cudaMemcpy(st, p->d_stats, sizeof(st), cudaMemcpyDeviceToHost));
+    for (int i = 0; i < n; ++i) out[i] += st[i];
+  }
+  return MPS_OK;
+}
+
 int mps_graph_stream(mps_graph* g, void** s) {
   if (!g || !s) return fail(MPS_ERR_ARG, "NULL argument");
   *s = (void*)g->L.stream;

@@ -39,6 +39,8 @@ struct Prec<float> {
   static constexpr bool refine = true;
   static constexpr int bisect_rounds = 16;
   static constexpr double ns_stop = 1e-4;  // last Newton-Schulz step leaves ~1.5 ns_stop^2 < eps
+  static constexpr double tri_flush = 1e-30;  // relative |column|^2 flushed in the tridiagonalisation
+  static constexpr double tiny = 1e-36;       // absolute |column|^2 below which no reflector is formed
 };
 template <>
 struct Prec<double> {
@@ -47,6 +49,8 @@ struct Prec<double> {
   static constexpr bool refine = false;
   static constexpr int bisect_rounds = 26;
   static constexpr double ns_stop = 1e-8;
+  static constexpr double tri_flush = 1e-60;
+  static constexpr double tiny = 1e-280;
 };
 
 __device__ __forceinline__ int pidx(int i, int j, int m) {  // i <= j
@@ -65,14 +69,18 @@ __device__ __forceinline__ void gset(cx<T>* Gp, int i, int j, int m, cx<T> v) {
     Gp[pidx(j, i, m)] = conj(v);
 }
 
-// Block-wide sum of a double; `red` holds >= 32 doubles of shared memory.
-__device__ double block_sum(double v, double* red) {
+// Block-wide sum in R (float or double); `red` holds >= 32 doubles of shared
+// memory.  FP64 runs at a small fraction of the FP32 rate on this part, so the
+// FP32 kernels sum in float.
+template <typename R>
+__device__ R block_sum(R v, double* red_d) {
+  R* red = reinterpret_cast<R*>(red_d);
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
   __syncthreads();
   if (l == 0) red[w] = v;
   __syncthreads();
-  double s = 0.0;
+  R s = R(0);
   const int nw = blockDim.x >> 5;
   for (int i = 0; i < nw; ++i) s += red[i];
   __syncthreads();
@@ -82,7 +90,7 @@ __device__ double block_sum(double v, double* red) {
 // Small per-CTA shared state that lives after the large arrays.
 template <typename T>
 struct SmallSmem {
-  double lam[kMaxM];
+  T lam[kMaxM];      // eigenvalues (working precision, from bisection)
   int perm[kMaxM];
   T iso[kMaxM];
   T oth[kMaxM];
@@ -100,6 +108,9 @@ struct SmallSmem {
   int ival[8];
   double dval[8];
 };
+
+static_assert((kOpThreads / 32) * sizeof(cx<double>) <= sizeof(double) * 32,
+              "per-warp complex partials must fit in SmallSmem::red");
 
 template <typename T>
 struct Layout {
@@ -131,35 +142,38 @@ __device__ void householder_qr(cx<T>* M, int mr, int nc, cx<T>* Rb, SmallSmem<T>
   const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
   const int k = mr < nc ? mr : nc;
   for (int j = 0; j < k; ++j) {
-    double s = 0.0;
-    for (int i = j + 1 + tid; i < mr; i += nt) s += (double)abs2(M[i * nc + j]);
-    s = block_sum(s, sm->red);
-    if (tid == 0) {
+    // warp 0: norm, reflector scalars (working precision) and the scaled column
+    if (warp == 0) {
+      T s = T(0);
+      for (int i = j + 1 + lane; i < mr; i += 32) s += abs2(M[i * nc + j]);
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
       const cx<T> alpha = M[j * nc + j];
-      const double ar = alpha.re, ai = alpha.im;
-      if (s == 0.0 && ai == 0.0) {
+      __syncwarp();  // every lane has read alpha before lane 0 overwrites it with beta
+      const T ar = alpha.re, ai = alpha.im;
+      const T nrm2 = ar * ar + ai * ai + s;
+      // a column below ~sqrt(tiny) is left as is (its reflector scale would overflow)
+      const bool refl = !(s == T(0) && ai == T(0)) && nrm2 > T(Prec<T>::tiny);
+      T ir = T(0), ii = T(0);
+      if (refl) {
+        const T beta = -copysign(sqrt(nrm2), ar);
+        const T dr = ar - beta, di = ai, den = dr * dr + di * di;
+        ir = dr / den;
+        ii = -di / den;
+        if (lane == 0) {
+          sm->tau[j] = mk<T>((beta - ar) / beta, -ai / beta);
+          M[j * nc + j] = mk<T>(beta, T(0));
+        }
+        for (int i = j + 1 + lane; i < mr; i += 32) {
+          const cx<T> x = M[i * nc + j];
+          M[i * nc + j] = mk<T>(x.re * ir - x.im * ii, x.re * ii + x.im * ir);
+        }
+      } else if (lane == 0) {
         sm->tau[j] = mk<T>(0, 0);
-        sm->ival[1] = 0;
-      } else {
-        const double beta = -copysign(sqrt(ar * ar + ai * ai + s), ar);
-        sm->tau[j] = mk<T>(T((beta - ar) / beta), T(-ai / beta));
-        // 1 / (alpha - beta)
-        const double dr = ar - beta, di = ai, den = dr * dr + di * di;
-        sm->dval[0] = dr / den;
-        sm->dval[1] = -di / den;
-        M[j * nc + j] = mk<T>(T(beta), T(0));
-        sm->ival[1] = 1;
       }
+      if (lane == 0) sm->ival[1] = refl ? 1 : 0;
     }
     __syncthreads();
     if (sm->ival[1]) {
-      // scale in double: 1/(alpha - beta) can exceed the range of T
-      const double ir = sm->dval[0], ii = sm->dval[1];
-      for (int i = j + 1 + tid; i < mr; i += nt) {
-        const cx<T> x = M[i * nc + j];
-        M[i * nc + j] = mk<T>(T((double)x.re * ir - (double)x.im * ii), T((double)x.re * ii + (double)x.im * ir));
-      }
-      __syncthreads();
       const cx<T> ctau = conj(sm->tau[j]);
       for (int c = j + 1 + warp; c < nc; c += nw) {
         cx<T> w = mk<T>(0, 0);
@@ -225,43 +239,41 @@ __device__ void householder_qr(cx<T>* M, int mr, int nc, cx<T>* Rb, SmallSmem<T>
 template <typename T>
 __device__ void tridiagonalize(cx<T>* A, int m, double trace, SmallSmem<T>* sm) {
   const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
-  // columns this small relative to the trace are flushed to zero, so the
-  // reflector scale 1/(alpha - beta) stays finite in T
-  const double flush2 = 1e-60 * trace * trace + 1e-74;
+  // columns this small relative to the trace carry eigen-weight below the
+  // working precision; they are flushed to zero so 1/(alpha - beta) stays finite
+  const T flush2 = T(Prec<T>::tri_flush * trace * trace + Prec<T>::tiny);
   for (int j = 0; j + 1 < m; ++j) {
     const int L = m - j - 1;  // x = A[j+1:m, j]
+    // warp 0: reflector of column j (scalars in working precision)
     if (warp == 0) {
-      double s = 0.0;
-      for (int i = 1 + lane; i < L; i += 32) s += (double)abs2(A[(j + 1 + i) * m + j]);
+      T s = T(0);
+      for (int i = 1 + lane; i < L; i += 32) s += abs2(A[(j + 1 + i) * m + j]);
       for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
       const cx<T> alpha = A[(j + 1) * m + j];
-      double ar = alpha.re, ai = alpha.im;
-      double nrm2 = ar * ar + ai * ai + s;
+      const T ar = alpha.re, ai = alpha.im;
+      const T nrm2 = ar * ar + ai * ai + s;
       const bool flush = nrm2 <= flush2;
-      if (flush) {
-        ar = ai = s = nrm2 = 0.0;
-      }
-      double beta = ar, tr = 0.0, ti = 0.0, ir = 0.0, ii = 0.0;
-      const bool refl = !((s == 0.0 && ai == 0.0) || nrm2 == 0.0);
+      const bool refl = !flush && !(s == T(0) && ai == T(0));
+      T beta = flush ? T(0) : ar, tr = T(0), ti = T(0), ir = T(0), ii = T(0);
       if (refl) {
         beta = -copysign(sqrt(nrm2), ar);
         tr = (beta - ar) / beta;
         ti = -ai / beta;
-        const double dr = ar - beta, di = ai, den = dr * dr + di * di;
+        const T dr = ar - beta, di = ai, den = dr * dr + di * di;
         ir = dr / den;
         ii = -di / den;
       }
       for (int i = lane; i < L; i += 32) {
         cx<T> v = mk<T>(T(i == 0), T(0));
-        if (i > 0 && refl && !flush) {
+        if (i > 0 && refl) {
           const cx<T> x = A[(j + 1 + i) * m + j];
-          v = mk<T>(T((double)x.re * ir - (double)x.im * ii), T((double)x.re * ii + (double)x.im * ir));
+          v = mk<T>(x.re * ir - x.im * ii, x.re * ii + x.im * ir);
         }
         sm->tv[i] = v;
       }
       if (lane == 0) {
-        sm->ttau[j] = mk<T>(T(tr), T(ti));
-        sm->te[j] = T(beta);
+        sm->ttau[j] = mk<T>(tr, ti);
+        sm->te[j] = beta;
       }
     }
     __syncthreads();
@@ -271,7 +283,7 @@ __device__ void tridiagonalize(cx<T>* A, int m, double trace, SmallSmem<T>* sm) 
       __syncthreads();
       continue;
     }
-    // p = tau * At v with At = A[j+1:, j+1:]; four lanes per row
+    // p = tau At v (At = A[j+1:, j+1:], four lanes per row) and d = p^H v
     {
       const int r = tid >> 2, q = tid & 3;
       cx<T> acc = mk<T>(0, 0);
@@ -283,27 +295,33 @@ __device__ void tridiagonalize(cx<T>* A, int m, double trace, SmallSmem<T>* sm) 
       acc.im += __shfl_xor_sync(0xffffffffu, acc.im, 1);
       acc.re += __shfl_xor_sync(0xffffffffu, acc.re, 2);
       acc.im += __shfl_xor_sync(0xffffffffu, acc.im, 2);
-      if (r < L && q == 0) sm->tp[r] = tau * acc;
-    }
-    __syncthreads();
-    // w = p - 1/2 tau (p^H v) v
-    if (warp == 0) {
-      cx<T> d = mk<T>(0, 0);
-      for (int i = lane; i < L; i += 32) fma_cj(d, sm->tp[i], sm->tv[i]);
-      for (int o = 16; o > 0; o >>= 1) {
-        d.re += __shfl_xor_sync(0xffffffffu, d.re, o);
-        d.im += __shfl_xor_sync(0xffffffffu, d.im, o);
+      cx<T> dpart = mk<T>(0, 0);
+      if (r < L && q == 0) {
+        const cx<T> p = tau * acc;
+        sm->tp[r] = p;
+        fma_cj(dpart, p, sm->tv[r]);
       }
-      const cx<T> a2 = scl(tau * d, T(-0.5));
-      __syncwarp();
-      for (int i = lane; i < L; i += 32) sm->tp[i] = sm->tp[i] + a2 * sm->tv[i];
+      for (int o = 16; o > 0; o >>= 1) {
+        dpart.re += __shfl_xor_sync(0xffffffffu, dpart.re, o);
+        dpart.im += __shfl_xor_sync(0xffffffffu, dpart.im, o);
+      }
+      // per-warp partials, summed below in a fixed order (reproducible results)
+      if (lane == 0) reinterpret_cast<cx<T>*>(sm->red)[warp] = dpart;
     }
     __syncthreads();
-    // At -= v w^H + w v^H
-    for (int t = tid; t < L * L; t += nt) {
-      const int r = t / L, c = t - r * L;
-      cx<T>& a = A[(j + 1 + r) * m + (j + 1 + c)];
-      a = a - (sm->tv[r] * conj(sm->tp[c]) + sm->tp[r] * conj(sm->tv[c]));
+    // At -= v w^H + w v^H with w = p - 1/2 tau (p^H v) v formed on the fly
+    {
+      cx<T> d = mk<T>(0, 0);
+      const cx<T>* part = reinterpret_cast<const cx<T>*>(sm->red);
+      for (int w = 0; w < (nt >> 5); ++w) d = d + part[w];
+      const cx<T> a2 = scl(tau * d, T(-0.5));
+      for (int t = tid; t < L * L; t += nt) {
+        const int r = t / L, c = t - r * L;
+        const cx<T> vr = sm->tv[r], vc = sm->tv[c];
+        const cx<T> wr = sm->tp[r] + a2 * vr, wc = sm->tp[c] + a2 * vc;
+        cx<T>& a = A[(j + 1 + r) * m + (j + 1 + c)];
+        a = a - (vr * conj(wc) + wr * conj(vc));
+      }
     }
     __syncthreads();
   }
@@ -391,7 +409,7 @@ __device__ void tri_bisect(int m, SmallSmem<T>* sm) {
       a = x3;
     }
   }
-  if (live && q == 0) sm->lam[j] = (double)(T(0.5) * (a + b));
+  if (live && q == 0) sm->lam[j] = T(0.5) * (a + b);
   __syncthreads();
 }
 
@@ -499,19 +517,21 @@ __device__ const cx<T>* orthonormalize(cx<T>* Wc, int m, int k, cx<T>* U, SmallS
   cx<T>* nxt = U + k * k;
   for (int it = 0; it < 5; ++it) {
     __syncthreads();
-    double f2 = 0.0;
+    T f2 = T(0);
     for (int t = tid; t < k * k; t += nt) {
       const int a = t / k, b = t - a * k;
       cx<T> acc = mk<T>(0, 0);
       for (int i = 0; i < m; ++i) fma_cj(acc, cur[i * k + a], cur[i * k + b]);
       if (a == b) acc.re -= T(1);
       E[t] = acc;
-      f2 += (double)abs2(acc);
+      f2 += abs2(acc);
     }
     // |E|_2 <= |E|_F: below 0.1 the steps converge quadratically
-    const double fro = sqrt(block_sum(f2, sm->red));
+    const double fro = sqrt((double)block_sum<T>(f2, sm->red));
     if (it == 0 && fro > 0.1) {
       householder_qr<T>(Wc, m, k, U, sm);
+      if (tid == 0) sm->ival[5] = 1;  // QR taken: vectors of a degenerate cluster
+      __syncthreads();
       return Wc;
     }
     for (int t = tid; t < m * k; t += nt) {
@@ -526,6 +546,8 @@ __device__ const cx<T>* orthonormalize(cx<T>* Wc, int m, int k, cx<T>* U, SmallS
     nxt = tmp;
     if (fro < Prec<T>::ns_stop) break;
   }
+  if (tid == 0) sm->ival[5] = 0;
+  __syncthreads();
   return cur;
 }
 
@@ -534,7 +556,7 @@ __device__ const cx<T>* orthonormalize(cx<T>* Wc, int m, int k, cx<T>* U, SmallS
 template <typename T>
 __device__ double gram_staged(const cx<T>* Xs, int m, int nn, int ld, cx<T>* Gp, SmallSmem<T>* sm) {
   const int tid = threadIdx.x, nt = blockDim.x;
-  double tr_part = 0.0;
+  T tr_part = T(0);
   const int nb = (m + 3) >> 2;
   const int ntiles = nb * (nb + 1) / 2;
   for (int tt = tid; tt < ntiles; tt += nt) {
@@ -576,38 +598,43 @@ __device__ double gram_staged(const cx<T>* Xs, int m, int nn, int ld, cx<T>* Gp,
           cx<T> v = acc[a][b];
           if (i == j) {
             v.im = T(0);
-            tr_part += (double)v.re;
+            tr_part += v.re;
           }
           Gp[pidx(i, j, m)] = v;
         }
       }
   }
-  return block_sum(tr_part, sm->red);
+  return (double)block_sum<T>(tr_part, sm->red);
 }
 
 // Eigenvalues of the packed Hermitian Gp (FP32 path): expanded into Af, reduced
 // to tridiagonal form (reflectors stay in Af), all eigenvalues by bisection
 // into sm->lam, and sm->perm ordering them descending.
 template <typename T>
-__device__ void eigvals_sorted(const cx<T>* Gp, cx<T>* Af, int m, double trace, SmallSmem<T>* sm) {
+__device__ void eigvals_sorted(const cx<T>* Gp, cx<T>* Af, int m, double trace, SmallSmem<T>* sm,
+                               long long& cyc_trid, long long& cyc_bisect) {
   const int tid = threadIdx.x, nt = blockDim.x;
+  const long long t0 = clock64();
   for (int t = tid; t < m * m; t += nt) {
     const int i = t / m, j = t - i * m;
     Af[t] = gget(Gp, i, j, m);
   }
   __syncthreads();
   tridiagonalize<T>(Af, m, trace, sm);
+  const long long t1 = clock64();
   tri_bisect<T>(m, sm);
   for (int i = tid; i < m; i += nt) {
-    const double li = sm->lam[i];
+    const T li = sm->lam[i];
     int rank = 0;
     for (int j = 0; j < m; ++j) {
-      const double lj = sm->lam[j];
+      const T lj = sm->lam[j];
       rank += (lj > li) || (lj == li && j < i);
     }
     sm->perm[rank] = i;
   }
   __syncthreads();
+  cyc_trid += t1 - t0;
+  cyc_bisect += clock64() - t1;
 }
 
 // Kept dimension for descending eigenvalues lam[0..mm) (squared singular
@@ -764,7 +791,8 @@ __device__ void op_gate2(const ProgDesc& P, const DevOp& op, char* big, SmallSme
   const long long c_gram = clock64();
   const int mm = R < Cc ? R : Cc;  // number of singular values (min(vol) in ExaTnMpsVisitor.cpp:1594)
   // reduce G (expanded into the U work matrix) to tridiagonal form
-  eigvals_sorted<T>(Gp, U, m, trace, sm);
+  long long cyc_trid = 0, cyc_bisect = 0, cyc_vec = 0, cyc_orth = 0;
+  eigvals_sorted<T>(Gp, U, m, trace, sm, cyc_trid, cyc_bisect);
   for (int r = tid; r < m; r += nt) sm->lk[r] = sm->lam[sm->perm[r]];
   __syncthreads();
   // FP32 small-eigenvalue refinement.  An FP32 Gram resolves eigenvalues only
@@ -790,13 +818,17 @@ __device__ void op_gate2(const ProgDesc& P, const DevOp& op, char* big, SmallSme
     __syncthreads();
     const int s = sm->ival[6];
     if (sm->ival[7]) {
+      const long long v0 = clock64();
       for (int c = tid; c < s; c += nt) {
         const int ev = sm->perm[c];
         tri_twisted<T>(Wc, m, s, c, T(sm->lam[ev]), sm->bs[ev], sm->bt[ev], sm);
       }
       __syncthreads();
       tri_backtransform<T>(U, Wc, m, s, s, sm);
+      const long long v1 = clock64();
       const cx<T>* Wh = orthonormalize<T>(Wc, m, s, U, sm);
+      cyc_vec += v1 - v0;
+      cyc_orth += clock64() - v1;
       for (int t = tid; t < m * s; t += nt) Wg[t] = Wh[t];
       __syncthreads();
       // Y_h = W_h^H X (s x nn) in the Gram region
@@ -819,7 +851,7 @@ __device__ void op_gate2(const ProgDesc& P, const DevOp& op, char* big, SmallSme
       }
       __syncthreads();
       const double trz = gram_staged<T>(Zs, m, nn, ld, Gp, sm);
-      eigvals_sorted<T>(Gp, U, m, trz, sm);
+      eigvals_sorted<T>(Gp, U, m, trz, sm, cyc_trid, cyc_bisect);
       for (int r = s + tid; r < m; r += nt) sm->lk[r] = sm->lam[sm->perm[r - s]];
       __syncthreads();
       refine_flops = 16.0 * m * s * nn + 8.0 * m * m * nn;
@@ -875,6 +907,8 @@ __device__ void op_gate2(const ProgDesc& P, const DevOp& op, char* big, SmallSme
   __syncthreads();
   // Kept eigenvectors W_k (m x k, ld k) in the Gram region.
   const cx<T>* W;
+  const long long c_vec = clock64();
+  long long c_orth = 0;
   {
     // twisted-factorisation vectors of the tridiagonal matrix, back-transformed
     // by the reflectors still held in the U work matrix; with the refinement,
@@ -920,14 +954,19 @@ __device__ void op_gate2(const ProgDesc& P, const DevOp& op, char* big, SmallSme
       __syncthreads();
       tri_backtransform<T>(U, Wc, m, k, k, sm);
     }
+    c_orth = clock64();
     W = orthonormalize<T>(Wc, m, k, U, sm);
-    if (Prec<T>::refine && k < m) {
+    if ((Prec<T>::refine || sm->ival[5]) && k < m) {
       // One subspace-iteration step W <- orth(X (X^H W)) with X itself, not
       // the FP32 Gram: the Gram's rounding (~eps * trace) tilts a kept
       // eigenvector into the discarded space by ~eps * trace / lambda, while
       // the product's rounding is ~eps * sigma_max / sigma relative, so the
       // weight lost to the cut drops from ~eps^2 trace^2 / lambda to
-      // ~eps^2 sigma_max^2 (the accuracy of a backward-stable SVD).
+      // ~eps^2 sigma_max^2 (the accuracy of a backward-stable SVD).  FP64
+      // takes the step only after the QR fallback: twisted vectors of an
+      // (exactly) degenerate cluster in one unreduced block can coincide, and
+      // the QR then fills the deficient columns with rounding-noise
+      // directions, which X X^H maps back onto the dominant subspace.
       cx<T>* Wk = Wg;                     // W copied out (m x k)
       cx<T>* Yv = Wg + kMaxM * kChiLimit;  // X^H W (nn x k)
       for (int t = tid; t < m * k; t += nt) Wk[t] = W[t];
@@ -947,19 +986,22 @@ __device__ void op_gate2(const ProgDesc& P, const DevOp& op, char* big, SmallSme
       }
       __syncthreads();
       for (int j = tid; j < k; j += nt) {
-        double s2 = 0.0;
-        for (int i = 0; i < m; ++i) s2 += (double)abs2(Wc[i * k + j]);
-        sm->lam[j] = s2;  // free after the eigenvector stage
+        T s2 = T(0);
+        for (int i = 0; i < m; ++i) s2 += abs2(Wc[i * k + j]);
+        // inverse column norm, 0 for a column that vanished (keep W's column)
+        sm->twv[j].re = s2 > T(Prec<T>::tiny) ? T(1) / sqrt(s2) : T(0);
       }
       __syncthreads();
       for (int t = tid; t < m * k; t += nt) {
         const int j = t - (t / k) * k;
-        const double s2 = sm->lam[j];
-        Wc[t] = s2 > 1e-60 ? scl(Wc[t], T(1.0 / sqrt(s2))) : Wk[t];
+        const T inv = sm->twv[j].re;
+        Wc[t] = inv > T(0) ? scl(Wc[t], inv) : Wk[t];
       }
       W = orthonormalize<T>(Wc, m, k, U, sm);
     }
   }
+  cyc_vec += c_orth - c_vec;
+  cyc_orth += clock64() - c_orth;
   // other side: Z = W_k^H X (k x nn)
   for (int t = tid; t < k * nn; t += nt) {
     const int j = t / nn, c = t - j * nn;
@@ -988,6 +1030,10 @@ __device__ void op_gate2(const ProgDesc& P, const DevOp& op, char* big, SmallSme
     P.stats[ST_CYC_GRAM] += (double)(c_gram - c_theta);
     P.stats[ST_CYC_EIG] += (double)(c_eig - c_gram);
     P.stats[ST_CYC_SPLIT] += (double)(c_end - c_eig);
+    P.stats[ST_CYC_TRID] += (double)cyc_trid;
+    P.stats[ST_CYC_BISECT] += (double)cyc_bisect;
+    P.stats[ST_CYC_VEC] += (double)cyc_vec;
+    P.stats[ST_CYC_ORTH] += (double)cyc_orth;
   }
 }
 
@@ -1163,6 +1209,7 @@ constexpr size_t kNoAllocHeader = 256;  // two site offsets, stats, error word
 constexpr size_t kNoAllocScratch = Layout<double>::scratch;  // largest per-CTA scratch (FP64)
 constexpr size_t kNoAllocBytes = kNoAllocHeader + kNoAllocScratch;  // 256 B + 512 KiB
 static __device__ __align__(256) char g_noalloc_scratch[kNoAllocBytes];
+static_assert(64 + sizeof(double) * ST_COUNT <= 192, "stats must end before the error word at 192");
 
 template <typename T>
 __global__ void __launch_bounds__(kOpThreads, 1) k_gate2_noalloc(ProgDesc P, DevOp op, char* scratch) {

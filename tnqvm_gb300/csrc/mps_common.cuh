@@ -87,14 +87,18 @@ enum StatSlot {
   ST_N_GATE2 = 2,     // number of 2-qubit gate splits
   ST_N_OPS = 3,       // number of ops executed
   ST_FLOPS = 4,       // GEMM-class flops: theta merge + gate + Gram + split + centre-move products
-  ST_EIG_FLOPS = 5,   // Jacobi rotations and Householder reflections
+  ST_EIG_FLOPS = 5,   // Householder reflections of the eigensolver and the centre-move QR
   ST_CYC_THETA = 6,   // SM clock cycles spent per phase (thread 0's clock64 deltas)
   ST_CYC_GRAM = 7,
   ST_CYC_EIG = 8,
   ST_CYC_SPLIT = 9,
   ST_CYC_MOVE = 10,
   ST_N_REFINE = 11,   // two-site splits whose small-eigenvalue block was re-solved
-  ST_COUNT = 12,
+  ST_CYC_TRID = 12,   // within the eigensolver: Householder tridiagonalisation
+  ST_CYC_BISECT = 13, //   bisection and ranking of the eigenvalues
+  ST_CYC_VEC = 14,    //   twisted-factorisation vectors and their back-transform
+  ST_CYC_ORTH = 15,   // orthonormalisation and the subspace step (within the split phase)
+  ST_COUNT = 16,
 };
 
 // Error bits written by the kernels into ProgDesc::err.

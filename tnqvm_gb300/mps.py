@@ -68,6 +68,7 @@ SIGNATURES = [
     ("mps_graph_destroy", _c.c_int, [_P]),
     ("mps_graph_timing", _c.c_int, [_P, _DP]),
     ("mps_graph_phase_cycles", _c.c_int, [_P, _DP]),
+    ("mps_graph_stat_sums", _c.c_int, [_P, _DP, _c.c_int]),
     ("mps_gates", _c.c_int, [_P, _c.c_int, _c.POINTER(_c.c_int32), _c.POINTER(_c.c_int32), _DP]),
     ("mps_gate2_apply_noalloc", _c.c_int, [_c.c_int, _c.c_int, _c.c_int, _c.c_double, _P, _c.c_int64,
                                             _P, _c.POINTER(_c.c_int), _DP, _P]),
@@ -238,6 +239,15 @@ class Graph:
         out = np.zeros(5)
         _check(_lib.mps_graph_phase_cycles(self.h, _dptr(out)))
         return dict(zip(["theta", "gram", "eigensolver", "split", "moves"], out.tolist()))
+
+    STAT_NAMES = ["log_fid", "max_disc", "gate2", "ops", "flops", "eig_flops", "cyc_theta", "cyc_gram",
+                  "cyc_eig", "cyc_split", "cyc_move", "refined", "cyc_trid", "cyc_bisect", "cyc_vec", "cyc_orth"]
+
+    def stat_sums(self):
+        """Per-program statistics of the last replay summed over the programs."""
+        out = np.zeros(16)
+        _check(_lib.mps_graph_stat_sums(self.h, _dptr(out), 16))
+        return dict(zip(self.STAT_NAMES, out.tolist()))
 
     @property
     def stream(self):
