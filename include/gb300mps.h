@@ -53,6 +53,9 @@ extern "C" {
 
 /* largest bond dimension the single-CTA gate kernel handles */
 #define MPS_CHI_LIMIT 64
+/* largest bond cap of a program; caps above MPS_CHI_LIMIT run the wide
+ * two-site path (tensor-core GEMMs, cooperative eigensolver and QR) */
+#define MPS_WIDE_CHI_LIMIT 1024
 /* largest qubit count for mps_amplitudes */
 #define MPS_AMP_QUBITS_MAX 26
 
@@ -77,8 +80,10 @@ int mps_ctx_info(mps_ctx* ctx, int* num_sms, size_t* bytes_resident);
  * Replaces ExatnMpsVisitor::initialize (ExaTnMpsVisitor.cpp:173-345) and
  * ITensorMPSVisitor::initialize (ITensorMPSVisitor.cpp:105-157):
  * |0...0> with every bond of dimension 1.  chi_max <= 0 means "no cap"
- * (clamped to MPS_CHI_LIMIT); cutoff < 0 selects the visitor's default
- * (DBL_MIN for exatn, 1e-6 for itensor). */
+ * (clamped to MPS_CHI_LIMIT); caps up to MPS_WIDE_CHI_LIMIT are accepted,
+ * those above MPS_CHI_LIMIT run gate by gate on the wide path (not with
+ * MPS_FLAG_PER_GATE, captured graphs or the serve loop).  cutoff < 0 selects
+ * the visitor's default (DBL_MIN for exatn, 1e-6 for itensor). */
 int mps_program_begin(mps_ctx* ctx, int n_qubits, int chi_max, double cutoff,
                       int trunc_mode, int precision, int flags, mps_prog** out);
 int mps_program_reset(mps_prog* p); /* back to |0...0>, keeps the allocation */
@@ -216,6 +221,15 @@ int mps_serve_stop(mps_ctx* ctx);
 int mps_gate2_apply_noalloc(int precision, int trunc_mode, int chi_max, double cutoff, void* sites,
                             int64_t hi_offset, int* d_bonds, const int* bonds, const double gate[32],
                             void* cuda_stream);
+
+/* Diagnostics of the wide path; no counterpart in the reference.
+ * mps_diag_cgemm: one complex64 product C = A B (M x K times K x N, host
+ * arrays of interleaved doubles, row-major) on the tensor-core kernel (c_tc)
+ * and on the CUDA-core kernel (c_simt).  mps_diag_gemm_counts: launches of
+ * each GEMM kernel by the wide path of this context so far. */
+int mps_diag_cgemm(mps_ctx* ctx, int M, int N, int K, const double* a, const double* b, double* c_tc,
+                   double* c_simt);
+int mps_diag_gemm_counts(mps_ctx* ctx, int* tensor_core, int* cuda_core);
 
 /* Footprint used by admission: sum over sites of chi_l * 2 * chi_r * bytes. */
 size_t mps_footprint_bytes(int n_qubits, int chi_max, int precision);

@@ -277,7 +277,7 @@ def test_serve_same_alone_and_in_mix(ctx):
 # ------------------------------------------------------- errors and edges
 def test_errors(ctx):
     with pytest.raises(M.MpsError) as e:
-        M.Program(ctx, 10, 65)
+        M.Program(ctx, 10, M.WIDE_CHI_LIMIT + 1)
     assert e.value.code == M.ERR_UNSUPPORTED
     with M.Program(ctx, 3) as p:
         with pytest.raises(M.MpsError) as e:

@@ -1,0 +1,143 @@
+"""GPU parity of the wide two-site path (bond caps above the single-CTA limit):
+tensor-core complex GEMMs, the cooperative eigensolver and QR, centre moves,
+GEMM-sweep expectations and sampling, called through the C ABI and checked
+against the CPU oracle.  Tolerances: 1e-10 for complex128 runs against the
+complex128 oracle (1e-8 for truncated exatn-mode runs, whose non-canonical
+Gram matrices square a larger condition number); 4e-6 relative (Frobenius)
+for one complex64 3xTF32 GEMM with K up to 1000; 1e-4 on amplitudes and 2e-5
+on expectation values for complex64 circuits."""
+import numpy as np
+import pytest
+
+from oracle import dense, routing
+from oracle import mps as omps
+from tnqvm_gb300 import circuits
+from tnqvm_gb300 import mps as M
+
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-10
+
+
+def run(ctx, n, circ, chi, cutoff, mode, prec, flags=0):
+    p = M.Program(ctx, n, chi, cutoff, mode, prec, flags)
+    p.run(circ)
+    p.submit()
+    p.wait()
+    return p
+
+
+def crand(rng, *shape):
+    return rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+
+
+@pytest.mark.parametrize("M_,N_,K_", [(128, 64, 16), (256, 128, 128), (300, 257, 129), (512, 512, 1000),
+                                      (1024, 96, 700)])
+def test_tensor_core_gemm(ctx, M_, N_, K_):
+    """3xTF32 tcgen05 product against complex128 numpy and the CUDA-core kernel."""
+    rng = np.random.default_rng(M_ + N_ + K_)
+    a = crand(rng, M_, K_)
+    b = crand(rng, K_, N_)
+    exact = a.astype(np.complex64).astype(np.complex128) @ b.astype(np.complex64).astype(np.complex128)
+    ct, cs = ctx.diag_cgemm(a, b)
+    scale = np.linalg.norm(exact)
+    assert np.linalg.norm(cs - exact) / scale < 1e-6
+    assert np.linalg.norm(ct - exact) / scale < 4e-6
+
+
+@pytest.mark.parametrize("mode", [M.TRUNC_EXATN, M.TRUNC_ITENSOR])
+def test_wide_exact_fp64(ctx, mode):
+    """14 qubits, brick wall depth 14, cap 128 (= exact): every amplitude and
+    <Z_i> against the dense oracle; bonds reach 128, so splits of a 256 x 256
+    theta run on the cooperative eigensolver."""
+    n = 14
+    circ = circuits.brickwall(n, 14, seed=21)
+    psi = dense.run(n, circ)
+    with run(ctx, n, circ, 128, 1e-14, mode, M.PREC_FP64) as p:
+        assert max(p.bond_dims()) == 128
+        amp = p.amplitudes()
+        assert np.max(np.abs(amp - psi)) < TOL64
+        zs = p.expect_pauli(["I" * q + "Z" + "I" * (n - q - 1) for q in range(n)])
+        for q in range(n):
+            assert abs(zs[q].real - dense.expect_z_parity(psi, [q])) < TOL64
+        assert abs(p.norm() - 1.0) < TOL64
+        bits = [(q * 7) % 2 for q in range(n)]
+        idx = sum(b << q for q, b in enumerate(bits))
+        assert abs(p.amplitude(bits) - psi[idx]) < TOL64
+
+
+@pytest.mark.parametrize("mode,omode", [(M.TRUNC_ITENSOR, "itensor"), (M.TRUNC_EXATN, "exatn")])
+def test_wide_truncated_fp64_vs_oracle(ctx, mode, omode):
+    """Cap 80 on 16 qubits (truncating, a non-power-of-two bond): bond
+    dimensions, Pauli expectations and truncation fidelity against the
+    complex128 oracle at the same cap and cutoff."""
+    n = 16
+    circ = circuits.brickwall(n, 12, seed=8)
+    ref = omps.run(n, routing.route(circ), mode=omode, chi_max=80, cutoff=1e-12)
+    rng = np.random.default_rng(3)
+    paulis, _ = circuits.random_paulis(n, 6, rng)
+    paulis = list(paulis) + ["I" * n]
+    with run(ctx, n, circ, 80, 1e-12, mode, M.PREC_FP64) as p:
+        assert p.bond_dims() == ref.bond_dims()
+        vals = p.expect_pauli(paulis)
+        tol = 1e-9 if mode == M.TRUNC_ITENSOR else 1e-8
+        for s, v in zip(paulis, vals):
+            assert abs(v - ref.expect_pauli(s)) < tol, s
+        assert abs(p.truncation_fidelity() - ref.fidelity) < 1e-9
+
+
+@pytest.mark.parametrize("mode", [M.TRUNC_EXATN, M.TRUNC_ITENSOR])
+def test_wide_exact_fp32(ctx, mode):
+    """complex64 wide path (tensor-core GEMMs) on the exact 14-qubit circuit."""
+    n = 14
+    circ = circuits.brickwall(n, 14, seed=21)
+    psi = dense.run(n, circ)
+    t0, _ = ctx.gemm_counts()
+    with run(ctx, n, circ, 128, 1e-14, mode, M.PREC_FP32) as p:
+        amp = p.amplitudes()
+        assert np.max(np.abs(amp - psi)) < 1e-4
+        zs = p.expect_pauli(["I" * q + "Z" + "I" * (n - q - 1) for q in range(n)])
+        for q in range(n):
+            assert abs(zs[q].real - dense.expect_z_parity(psi, [q])) < 2e-5
+    t1, _ = ctx.gemm_counts()
+    assert t1 > t0  # the tensor-core kernel ran
+
+
+def test_wide_routed_itensor_fp64(ctx):
+    """Non-adjacent gates (SWAP routing) and centre moves in both directions:
+    a 3-regular QAOA circuit on 14 qubits, cap 100, against the oracle."""
+    n = 14
+    circ, _ = circuits.qaoa_maxcut(n, 1, seed=3)
+    ref = omps.run(n, routing.route(circ), mode="itensor", chi_max=100, cutoff=1e-12)
+    with run(ctx, n, circ, 100, 1e-12, M.TRUNC_ITENSOR, M.PREC_FP64) as p:
+        assert p.bond_dims() == ref.bond_dims()
+        for s in ["Z" * n, "ZZ" + "I" * (n - 2), "I" * (n - 2) + "XX", "Y" + "I" * (n - 2) + "Y"]:
+            assert abs(p.expect_pauli([s])[0] - ref.expect_pauli(s)) < 1e-9, s
+
+
+def test_wide_sampling_chi_square(ctx):
+    """4096 shots of a 10-qubit state held at cap 96 against the exact
+    probabilities (chi-square, p > 1e-4)."""
+    from scipy import stats
+    n = 10
+    circ = circuits.brickwall(n, 6, seed=4)
+    psi = dense.run(n, circ)
+    probs = np.abs(psi) ** 2
+    with run(ctx, n, circ, 96, 1e-14, M.TRUNC_EXATN, M.PREC_FP64) as p:
+        bits = p.sample(4096, seed=17)
+    idx = (bits.astype(np.int64) << np.arange(n)).sum(axis=1)
+    counts = np.bincount(idx, minlength=1 << n)
+    big = probs * 4096 >= 5
+    obs = np.append(counts[big], counts[~big].sum())
+    exp = np.append(probs[big], probs[~big].sum()) * 4096
+    chi2 = ((obs - exp) ** 2 / np.maximum(exp, 1e-300)).sum()
+    assert stats.chi2.sf(chi2, len(obs) - 1) > 1e-4
+
+
+def test_wide_rejections(ctx):
+    with pytest.raises(M.MpsError) as e:
+        M.Program(ctx, 20, 2048, -1.0, M.TRUNC_EXATN, M.PREC_FP32)
+    assert e.value.code == M.ERR_UNSUPPORTED
+    with pytest.raises(M.MpsError) as e:
+        M.Program(ctx, 20, 128, -1.0, M.TRUNC_EXATN, M.PREC_FP64, M.FLAG_PER_GATE)
+    assert e.value.code == M.ERR_UNSUPPORTED

@@ -221,7 +221,21 @@ static int ensure_bytes(char** ptr, int* have, int need, size_t per) {
 // Compile, upload and launch.  Non per-gate: one persistent launch whose CTAs
 // pull whole programs from an atomic queue (longest first).  Per-gate: one
 // single-CTA launch per op, the plain gate-by-gate visitor path.
-int launch_programs(mps_ctx* c, Lane& L, mps_prog* const* progs, int n, bool per_gate) {
+int launch_programs(mps_ctx* c, Lane& L, mps_prog* const* progs_in, int n_in, bool per_gate) {
+  // wide programs run host-driven on this lane, one after the other
+  std::vector<mps_prog*> narrow;
+  narrow.reserve(n_in);
+  for (int i = 0; i < n_in; ++i) {
+    if (prog_is_wide(progs_in[i])) {
+      const int rc = wide_run(c, L, progs_in[i]);
+      if (rc) return rc;
+    } else {
+      narrow.push_back(progs_in[i]);
+    }
+  }
+  mps_prog* const* progs = narrow.data();
+  const int n = (int)narrow.size();
+  if (n == 0) return MPS_OK;
   std::vector<std::vector<DevOp>> all(n);
   size_t total = 0;
   int prec = -1;
@@ -504,6 +518,7 @@ int mps_ctx_destroy(mps_ctx* c) {
   mps_serve_stop(c);
   cudaSetDevice(c->device);
   lane_free(c->lane0);
+  wide_free(c);
   delete c;
   return MPS_OK;
 }
@@ -539,6 +554,7 @@ static int init_state(mps_prog* p) {
   CK(cudaMemsetAsync(p->d_stats, 0, ST_COUNT * sizeof(double), st));
   CK(cudaMemsetAsync(p->d_err, 0, sizeof(int), st));
   CK(cudaStreamSynchronize(st));
+  p->hbond.assign(p->n + 1, 1);
   p->center = 0;
   p->pending.clear();
   p->measured.clear();
@@ -553,9 +569,11 @@ int mps_program_begin(mps_ctx* c, int n, int chi_max, double cutoff, int trunc_m
   if (n < 1) return fail(MPS_ERR_ARG, "n_qubits must be >= 1");
   if (trunc_mode != MPS_TRUNC_EXATN && trunc_mode != MPS_TRUNC_ITENSOR) return fail(MPS_ERR_ARG, "bad trunc_mode");
   if (precision != MPS_PREC_FP64 && precision != MPS_PREC_FP32) return fail(MPS_ERR_ARG, "bad precision");
-  if (chi_max > MPS_CHI_LIMIT)
-    return fail(MPS_ERR_UNSUPPORTED, "max bond dimension above " + std::to_string(MPS_CHI_LIMIT) +
-                                         " needs a multi-CTA split, which this build does not have");
+  if (chi_max > MPS_WIDE_CHI_LIMIT)
+    return fail(MPS_ERR_UNSUPPORTED, "max bond dimension above " + std::to_string(MPS_WIDE_CHI_LIMIT));
+  if (chi_max > MPS_CHI_LIMIT && (flags & MPS_FLAG_PER_GATE))
+    return fail(MPS_ERR_UNSUPPORTED, "the per-gate visitor path runs the single-CTA kernel (bond cap <= " +
+                                         std::to_string(MPS_CHI_LIMIT) + ")");
   if (chi_max <= 0) chi_max = MPS_CHI_LIMIT;
   std::lock_guard<std::mutex> lk(c->mu);
   CK(cudaSetDevice(c->device));
@@ -753,6 +771,19 @@ int mps_expect_pauli(mps_prog* p, const char* paulis, int n_terms, const double*
     if (coeffs) out[0] = 0.0;
     return MPS_OK;
   }
+  if (prog_is_wide(p)) {
+    std::vector<double> res(2 * (size_t)n_terms);
+    rc = wide_expect(p, codes.data(), n_terms, res.data());
+    if (rc) return rc;
+    double e = 0.0;
+    for (int t = 0; t < n_terms; ++t) {
+      out[2 * t] = res[2 * t];
+      out[2 * t + 1] = res[2 * t + 1];
+      if (coeffs) e += coeffs[t] * res[2 * t];
+    }
+    if (coeffs) out[2 * n_terms] = e;
+    return prog_check_err(p);
+  }
   uint8_t* d_codes = nullptr;
   CK(cudaMalloc(&d_codes, codes.size()));
   CK(cudaMemcpyAsync(d_codes, codes.data(), codes.size(), cudaMemcpyHostToDevice, c->lane0.stream));
@@ -811,6 +842,7 @@ int mps_set_observable(mps_prog* p, const char* paulis, int n_terms, const doubl
   CK(cudaMalloc(&p->d_obs, codes.size()));
   CK(cudaMemcpy(p->d_obs, codes.data(), codes.size(), cudaMemcpyHostToDevice));
   p->obs_coef.assign(coeffs, coeffs + n_terms);
+  p->obs_codes = codes;
   p->n_terms = n_terms;
   return MPS_OK;
 }
@@ -827,6 +859,7 @@ int mps_batch_expect(mps_ctx* c, mps_prog* const* progs, int n, double* out) {
     if (!p->d_obs) return fail(MPS_ERR_STATE, "program has no observable");
     int rc = flush_pending(p);
     if (rc) return rc;
+    if (prog_is_wide(p)) continue;
     where[i] = {p->prec, tasks[p->prec].size()};
     observable_tasks(p, tasks[p->prec]);
   }
@@ -840,6 +873,13 @@ int mps_batch_expect(mps_ctx* c, mps_prog* const* progs, int n, double* out) {
   for (int i = 0; i < n; ++i) {
     int rc = prog_check_err(progs[i]);
     if (rc) return rc;
+    if (prog_is_wide(progs[i])) {
+      std::vector<double> r(2 * ((size_t)progs[i]->n_terms + 1));
+      rc = wide_expect(progs[i], progs[i]->obs_codes.data(), progs[i]->n_terms + 1, r.data());
+      if (rc) return rc;
+      out[i] = observable_value(progs[i], r.data());
+      continue;
+    }
     out[i] = observable_value(progs[i], res[where[i].first].data() + 2 * where[i].second);
   }
   return MPS_OK;
@@ -894,6 +934,11 @@ int mps_amplitude(mps_prog* p, const int* bits, double out[2]) {
   CK(cudaSetDevice(c->device));
   int rc = flush_pending(p);
   if (rc) return rc;
+  if (prog_is_wide(p)) {
+    rc = wide_amp_one(p, bits, out);
+    if (rc) return rc;
+    return prog_check_err(p);
+  }
   cudaStream_t st = c->lane0.stream;
   char* buf = nullptr;
   CK(cudaMalloc(&buf, sizeof(int) * p->n + 16));
@@ -922,7 +967,10 @@ int mps_sample(mps_prog* p, int shots, uint64_t seed, uint8_t* bits) {
   int rc = flush_pending(p);
   if (rc) return rc;
   std::vector<uint8_t> all((size_t)shots * p->n);
-  rc = enqueue_sample(c->lane0, p, shots, seed, all.data());
+  if (prog_is_wide(p))
+    rc = wide_sample(p, shots, seed, all.data());
+  else
+    rc = enqueue_sample(c->lane0, p, shots, seed, all.data());
   if (rc) return rc;
   CK(cudaStreamSynchronize(c->lane0.stream));
   rc = prog_check_err(p);
@@ -954,6 +1002,19 @@ int mps_truncation_fidelity(mps_prog* p, double* out) {
   if (rc) return rc;
   *out = st[0];
   return MPS_OK;
+}
+
+int mps_diag_cgemm(mps_ctx* c, int M, int N, int K, const double* a, const double* b, double* c_tc, double* c_simt) {
+  if (!c || !a || !b || !c_tc || !c_simt || M < 1 || N < 1 || K < 1 || M > 4096 || N > 4096 || K > 4096)
+    return fail(MPS_ERR_ARG, "bad argument");
+  std::lock_guard<std::mutex> lk(c->mu);
+  CK(cudaSetDevice(c->device));
+  return wide_diag_cgemm(c, M, N, K, a, b, c_tc, c_simt);
+}
+
+int mps_diag_gemm_counts(mps_ctx* c, int* tensor_core, int* cuda_core) {
+  if (!c || !tensor_core || !cuda_core) return fail(MPS_ERR_ARG, "NULL argument");
+  return wide_gemm_counts(c, tensor_core, cuda_core);
 }
 
 int mps_bond_dims(mps_prog* p, int* out) {

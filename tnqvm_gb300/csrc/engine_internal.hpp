@@ -115,6 +115,7 @@ struct mps_ctx {
   std::mutex mu;
   gbmps::Lane lane0;
   gbmps::ServeState* serve = nullptr;
+  void* wide = nullptr;  // workspace of the wide two-site path (wide.cu)
 };
 
 struct mps_prog {
@@ -137,7 +138,9 @@ struct mps_prog {
   int center = 0;
   uint8_t* d_obs = nullptr;
   std::vector<double> obs_coef;
+  std::vector<uint8_t> obs_codes;  // host copy of the observable (wide programs)
   int n_terms = 0;
+  std::vector<int> hbond;  // host mirror of the bond dimensions (wide programs)
 };
 
 namespace gbmps {
@@ -155,4 +158,14 @@ int parse_paulis(int n, const char* paulis, int n_terms, std::vector<uint8_t>& c
 void select_measured(const ::mps_prog* p, const uint8_t* all, int shots, uint8_t* bits);
 void observable_tasks(::mps_prog* p, std::vector<ExpTask>& tasks);
 double observable_value(const ::mps_prog* p, const double* r);
+// wide path (wide.cu): bond caps above the single-CTA limit
+bool prog_is_wide(const ::mps_prog* p);
+int wide_run(mps_ctx* c, Lane& L, ::mps_prog* p);
+int wide_expect(::mps_prog* p, const uint8_t* codes, int n_terms, double* out);
+int wide_sample(::mps_prog* p, int shots, uint64_t seed, uint8_t* h_all_bits);
+int wide_amp_one(::mps_prog* p, const int* bits, double* out);
+int wide_gemm_counts(mps_ctx* c, int* tc, int* simt);
+int wide_diag_cgemm(mps_ctx* c, int M, int N, int K, const double* a, const double* b, double* out_tc,
+                    double* out_simt);
+void wide_free(mps_ctx* c);
 }  // namespace gbmps

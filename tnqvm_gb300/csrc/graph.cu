@@ -74,6 +74,8 @@ int mps_graph_create(mps_ctx* c, mps_prog* const* progs, int n, mps_graph** out)
   for (int i = 0; i < n; ++i) {
     if (!progs[i] || progs[i]->ctx != c) return fail(MPS_ERR_ARG, "program from another context");
     if (progs[i]->prec != progs[0]->prec) return fail(MPS_ERR_ARG, "batch mixes precisions");
+    if (prog_is_wide(progs[i]))
+      return fail(MPS_ERR_UNSUPPORTED, "captured batches hold single-CTA programs (bond cap <= 64)");
   }
   std::lock_guard<std::mutex> lk(c->mu);
   GCK(cudaSetDevice(c->device));

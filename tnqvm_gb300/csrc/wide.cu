@@ -1,0 +1,754 @@
+// Host-driven executor of wide programs (bond cap above the single-CTA limit).
+//
+// A wide program runs its compiled ops (routing, 1-qubit fusion and gauge
+// moves as for every program) one at a time on the lane's stream; the host
+// mirrors the bond dimensions and reads the kept dimension back after each
+// split (one small copy per two-qubit gate, negligible next to a split of a
+// 2chi x 2chi theta).  Two-site update (ExaTnMpsVisitor.cpp:1387-1730 with
+// truncateSvdTensors :2366-2536; ITensorMPSVisitor.cpp:312-331 with ITensor
+// truncate decomp.cc:307-463):
+//   T = A.B (GEMM), theta = gate(T), G = X X^H on the isometric side (GEMM),
+//   eigen-decomposition + keep rule (k_wide_eig), [complex64: one subspace
+//   step W <- X (X^H W)], orthonormalisation (Newton-Schulz GEMMs, or the
+//   cooperative QR for a degenerate cluster), isometric site W_k, other site
+//   W_k^H X (GEMM).
+// Centre moves (ITensor MPS::position) use the cooperative QR plus one GEMM.
+// Pauli expectations (ITensorMPSVisitor.cpp:173-250) and shot sampling
+// (ExaTnMpsVisitor.cpp:2211-2364) are transfer-matrix sweeps of GEMMs.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/gb300mps.h"
+#include "engine_internal.hpp"
+#include "wide.hpp"
+
+namespace gbmps {
+
+struct G16 {
+  double m[32];
+};
+
+template <typename T>
+__global__ void k_theta_gate(const cx<T>* __restrict__ Tb, cx<T>* __restrict__ Th, int dl, int dr, G16 g) {
+  const int Cc = 2 * dr;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < (int64_t)dl * dr;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int l = (int)(idx / dr), r = (int)(idx - (int64_t)l * dr);
+    cx<T> t[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) t[q] = Tb[(int64_t)(2 * l + (q >> 1)) * Cc + (q & 1) * dr + r];
+#pragma unroll
+    for (int row = 0; row < 4; ++row) {
+      cx<T> acc = mk<T>(T(0), T(0));
+#pragma unroll
+      for (int col = 0; col < 4; ++col)
+        fma_c(acc, mk<T>(T(g.m[2 * (row * 4 + col)]), T(g.m[2 * (row * 4 + col) + 1])), t[col]);
+      Th[(int64_t)(2 * l + (row >> 1)) * Cc + (row & 1) * dr + r] = acc;
+    }
+  }
+}
+
+template <typename T>
+__global__ void k_wide_gate1(cx<T>* A, int dl, int dr, G16 g) {
+  const cx<T> g00 = mk<T>(T(g.m[0]), T(g.m[1])), g01 = mk<T>(T(g.m[2]), T(g.m[3]));
+  const cx<T> g10 = mk<T>(T(g.m[4]), T(g.m[5])), g11 = mk<T>(T(g.m[6]), T(g.m[7]));
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < (int64_t)dl * dr;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int l = (int)(idx / dr), r = (int)(idx - (int64_t)l * dr);
+    const cx<T> a0 = A[(int64_t)(l * 2) * dr + r], a1 = A[(int64_t)(l * 2 + 1) * dr + r];
+    A[(int64_t)(l * 2) * dr + r] = g00 * a0 + g01 * a1;
+    A[(int64_t)(l * 2 + 1) * dr + r] = g10 * a0 + g11 * a1;
+  }
+}
+
+// Split scales: exatn puts sqrt(S) on both sides, itensor leaves the
+// isometric side as is; renormalisation rescales the kept part to the
+// pre-truncation norm.
+template <typename T>
+__global__ void k_split_scales(const double* lam, const WideEigStatus* st, int sqrt_mode, int renorm, T* iso,
+                               T* oth) {
+  const int k = st->k;
+  const double rn = (renorm && st->kept > 0.0) ? sqrt(st->total / st->kept) : 1.0;
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < k; j += gridDim.x * blockDim.x) {
+    const double v = lam[j];
+    const double sv = v > 0.0 ? sqrt(v) : 0.0;
+    if (sqrt_mode) {
+      const double h = sqrt(sv);
+      iso[j] = T(h);
+      oth[j] = T(h > 0.0 ? rn / h : 0.0);
+    } else {
+      iso[j] = T(1);
+      oth[j] = T(rn);
+    }
+  }
+}
+
+// Isometric site from W (m x k): plain (dst[i*k + j]) or transposed
+// (dst[j*m + i]); and Wo = W diag(oth) for the other side.
+template <typename T>
+__global__ void k_write_iso(const cx<T>* W, int m, int k, const T* iso, const T* oth, int transpose, cx<T>* dst,
+                            cx<T>* Wo) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < (int64_t)m * k;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(t / k), j = (int)(t - (int64_t)i * k);
+    const cx<T> w = W[t];
+    if (transpose)
+      dst[(int64_t)j * m + i] = scl(w, iso[j]);
+    else
+      dst[t] = scl(w, iso[j]);
+    Wo[t] = scl(w, oth[j]);
+  }
+}
+
+// |S - I|_F of a k x k matrix (one block).
+template <typename T>
+__global__ void k_defect(const cx<T>* S, int k, double* out) {
+  __shared__ double red[32];
+  double s = 0.0;
+  for (int64_t t = threadIdx.x; t < (int64_t)k * k; t += blockDim.x) {
+    const int a = (int)(t / k), b = (int)(t - (int64_t)a * k);
+    cx<T> z = S[t];
+    if (a == b) z.re -= T(1);
+    s += (double)abs2(z);
+  }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double tot = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += red[w];
+    *out = sqrt(tot);
+  }
+}
+
+// Column normalisation of W2 (m x k, ld k); a vanished column takes the
+// column of Wf (ld ldf) instead.
+template <typename T>
+__global__ void k_colnorm(cx<T>* W2, int m, int k, const cx<T>* Wf, int ldf, T* inv) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= k) return;
+  T s2 = T(0);
+  for (int i = 0; i < m; ++i) s2 += abs2(W2[(int64_t)i * k + j]);
+  const T tiny = sizeof(T) == 4 ? T(1e-36) : T(1e-280);
+  inv[j] = s2 > tiny ? T(1) / sqrt(s2) : T(0);
+  if (!(s2 > tiny))
+    for (int i = 0; i < m; ++i) W2[(int64_t)i * k + j] = Wf[(int64_t)i * ldf + j];
+}
+template <typename T>
+__global__ void k_colscale(cx<T>* W2, int m, int k, const T* inv) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < (int64_t)m * k;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int j = (int)(t % k);
+    if (inv[j] > T(0)) W2[t] = scl(W2[t], inv[j]);
+  }
+}
+
+// Statistics of a wide split (same slots as the single-CTA kernel) and the
+// new bond dimension.
+__global__ void k_wide_commit(double* stats, int* bond, int b, const WideEigStatus* st, double flops,
+                              double eig_flops) {
+  const double total = st->total, kept = st->kept;
+  const double frac = total > 0.0 ? (total - kept) / total : 0.0;
+  stats[ST_LOG_FID] += log1p(-(frac < 1.0 ? frac : 0.0));
+  if (frac > stats[ST_MAX_DISC]) stats[ST_MAX_DISC] = frac;
+  stats[ST_N_GATE2] += 1.0;
+  stats[ST_N_OPS] += 1.0;
+  stats[ST_FLOPS] += flops;
+  stats[ST_EIG_FLOPS] += eig_flops;
+  bond[b] = st->k;
+}
+__global__ void k_set_bond(double* stats, int* bond, int b, int v, double flops) {
+  if (b >= 0) bond[b] = v;
+  stats[ST_N_OPS] += 1.0;
+  stats[ST_FLOPS] += flops;
+}
+
+// H[l, s', r] = sum_s P[s'][s] F[l, s, r] for one Pauli (1 X, 2 Y, 3 Z).
+template <typename T>
+__global__ void k_pauli(const cx<T>* F, cx<T>* H, int dl, int dr, int code) {
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < (int64_t)dl * dr;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int l = (int)(idx / dr), r = (int)(idx - (int64_t)l * dr);
+    const cx<T> f0 = F[(int64_t)(2 * l) * dr + r], f1 = F[(int64_t)(2 * l + 1) * dr + r];
+    cx<T> h0, h1;
+    if (code == 1) {
+      h0 = f1;
+      h1 = f0;
+    } else if (code == 2) {  // Y = [[0, -i], [i, 0]]
+      h0 = mk<T>(f1.im, -f1.re);
+      h1 = mk<T>(-f0.im, f0.re);
+    } else {
+      h0 = f0;
+      h1 = mk<T>(-f1.re, -f1.im);
+    }
+    H[(int64_t)(2 * l) * dr + r] = h0;
+    H[(int64_t)(2 * l + 1) * dr + r] = h1;
+  }
+}
+
+template <typename T>
+__global__ void k_store_scalar(const cx<T>* E, double* out) {
+  out[0] = (double)E[0].re;
+  out[1] = (double)E[0].im;
+}
+
+// Philox4x32-10 (Salmon et al., SC'11) uniform in [0, 1) for (shot, site).
+__device__ __forceinline__ double wide_uniform(uint64_t seed, uint32_t shot, uint32_t site) {
+  uint4 c = make_uint4(shot, site, 0x57494445u, 0u);
+  uint2 k = make_uint2((uint32_t)seed, (uint32_t)(seed >> 32));
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    const uint32_t hi0 = __umulhi(0xD2511F53u, c.x), lo0 = 0xD2511F53u * c.x;
+    const uint32_t hi1 = __umulhi(0xCD9E8D57u, c.z), lo1 = 0xCD9E8D57u * c.z;
+    c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
+    k.x += 0x9E3779B9u;
+    k.y += 0xBB67AE85u;
+  }
+  const uint64_t v = ((uint64_t)c.x << 32) | c.y;
+  return (double)(v >> 11) * (1.0 / 9007199254740992.0);
+}
+
+// One site of shot sampling: U (S x 2dr, cols (s, r)) = V A, Q = U R_{i+1}
+// (rows (shot, s)); p_s = Re <U_s, Q_s>; bit 0 when u <= p0 / (p0 + p1)
+// (ExaTnMpsVisitor.cpp:2342-2345); V <- U_bit / sqrt(p_bit).  One warp per shot.
+template <typename T>
+__global__ void k_wide_sample_step(const cx<T>* U, const cx<T>* Q, cx<T>* V, int shots, int dr, int site, int n,
+                                   uint64_t seed, uint8_t* bits) {
+  const int lane = threadIdx.x & 31;
+  const int shot = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (shot >= shots) return;
+  const cx<T>* u = U + (int64_t)shot * 2 * dr;
+  const cx<T>* q = Q + (int64_t)shot * 2 * dr;
+  double p[2] = {0.0, 0.0};
+  for (int s = 0; s < 2; ++s) {
+    double acc = 0.0;
+    for (int r = lane; r < dr; r += 32) {
+      const cx<T> a = u[s * dr + r], b = q[s * dr + r];
+      acc += (double)a.re * b.re + (double)a.im * b.im;
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    p[s] = acc > 0.0 ? acc : 0.0;
+  }
+  const double tot = p[0] + p[1];
+  const double uu = wide_uniform(seed, (uint32_t)shot, (uint32_t)site);
+  const int bit = (tot > 0.0 && uu > p[0] / tot) ? 1 : 0;
+  const double inv = p[bit] > 0.0 ? 1.0 / sqrt(p[bit]) : 0.0;
+  for (int r = lane; r < dr; r += 32) V[(int64_t)shot * dr + r] = scl(u[bit * dr + r], T(inv));
+  if (lane == 0) bits[(int64_t)shot * n + site] = (uint8_t)bit;
+}
+
+// ------------------------------------------------------------ workspace
+struct WideBufs {
+  int prec = -1;
+  int m = 0;  // sized for Gram side m
+  void* theta = nullptr;
+  void* tbuf = nullptr;
+  void* gram = nullptr;
+  void* W = nullptr;
+  void* W2 = nullptr;
+  void* W3 = nullptr;
+  void* Y = nullptr;
+  void* S = nullptr;
+  void* R = nullptr;
+  void* scal = nullptr;  // iso, oth, inv (3 m of T)
+  double* lam = nullptr;
+  void* eig_work = nullptr;
+  void* qr_work = nullptr;
+  WideEigStatus* d_status = nullptr;
+  double* d_scalar = nullptr;  // 2 doubles
+  int* d_err = nullptr;
+  char* h_pinned = nullptr;  // status + scalars
+  GemmWs gemm;
+};
+
+struct WideAll {
+  WideBufs b[2];
+};
+
+static void wide_bufs_free(WideBufs& B) {
+  void* ptrs[] = {B.theta, B.tbuf, B.gram, B.W, B.W2, B.W3, B.Y, B.S, B.R, B.scal, B.lam, B.eig_work, B.qr_work,
+                  B.d_status, B.d_scalar, B.d_err};
+  for (void* q : ptrs)
+    if (q) cudaFree(q);
+  if (B.h_pinned) cudaFreeHost(B.h_pinned);
+  gemm_ws_free(B.gemm);
+  B = WideBufs();
+}
+
+void wide_free(mps_ctx* c) {
+  if (!c->wide) return;
+  WideAll* w = reinterpret_cast<WideAll*>(c->wide);
+  for (auto& b : w->b) wide_bufs_free(b);
+  delete w;
+  c->wide = nullptr;
+}
+
+static int wide_bufs(mps_ctx* c, int prec, int chi, WideBufs** out) {
+  if (!c->wide) c->wide = new WideAll();
+  WideBufs& B = reinterpret_cast<WideAll*>(c->wide)->b[prec];
+  const int m = 2 * chi;
+  if (B.prec == prec && B.m >= m) {
+    *out = &B;
+    return MPS_OK;
+  }
+  wide_bufs_free(B);
+  const size_t eb = prec == MPS_PREC_FP64 ? 16 : 8;
+  const size_t E = (size_t)m * m;
+  void** big[] = {&B.theta, &B.tbuf, &B.gram, &B.W, &B.W2, &B.W3, &B.Y, &B.S, &B.R};
+  bool ok = true;
+  for (void** q : big) ok = ok && cudaMalloc(q, E * eb) == cudaSuccess;
+  ok = ok && cudaMalloc(&B.scal, 3 * (size_t)m * eb) == cudaSuccess;
+  ok = ok && cudaMalloc(&B.lam, (size_t)m * sizeof(double)) == cudaSuccess;
+  ok = ok && cudaMalloc(&B.eig_work, wide_eig_work_bytes(prec, m)) == cudaSuccess;
+  ok = ok && cudaMalloc(&B.qr_work, wide_qr_work_bytes(prec, m, m)) == cudaSuccess;
+  ok = ok && cudaMalloc(&B.d_status, sizeof(WideEigStatus)) == cudaSuccess;
+  ok = ok && cudaMalloc(&B.d_scalar, 4 * sizeof(double)) == cudaSuccess;
+  ok = ok && cudaMalloc(&B.d_err, sizeof(int)) == cudaSuccess;
+  ok = ok && cudaMallocHost(&B.h_pinned, 256) == cudaSuccess;
+  // tensor-core operands: A side up to m x 2m, B side up to 2m x 2m (padded)
+  if (ok && prec == MPS_PREC_FP32) {
+    const size_t pad = (size_t)(m + 128) * (2 * m + 128);
+    ok = gemm_ws_init(B.gemm, pad, 2 * pad) == 0;
+  } else if (ok) {
+    ok = gemm_ws_init(B.gemm, 1, 1) == 0;
+  }
+  if (!ok) {
+    cudaGetLastError();
+    wide_bufs_free(B);
+    return fail(MPS_ERR_OOM, "wide-path workspace allocation failed");
+  }
+  cudaMemset(B.d_err, 0, sizeof(int));
+  B.prec = prec;
+  B.m = m;
+  *out = &B;
+  return MPS_OK;
+}
+
+#define WCK(call)                                                             \
+  do {                                                                        \
+    cudaError_t e_ = (call);                                                  \
+    if (e_ != cudaSuccess) return fail(MPS_ERR_CUDA, cudaGetErrorString(e_)); \
+  } while (0)
+
+static int blocks_for(int64_t n) { return (int)std::min<int64_t>((n + 255) / 256, 4096); }
+
+// ------------------------------------------------------------ two-site update
+template <typename T>
+static int orthonormalize_w(WideBufs& B, const CMat<T>& X, int m, int nn, int k, cx<T>* Wc, bool subspace,
+                            cudaStream_t st, cx<T>** result, double* ortho_flops) {
+  // Wc: m x k (ld k).  Returns the orthonormal columns in *result (ld k).
+  cx<T>* cur = Wc;
+  cx<T>* nxt = reinterpret_cast<cx<T>*>(cur == B.W3 ? B.W2 : B.W3);
+  cx<T>* S = reinterpret_cast<cx<T>*>(B.S);
+  double* hs = reinterpret_cast<double*>(B.h_pinned + 128);
+  const double ns_stop = sizeof(T) == 4 ? 1e-4 : 1e-8;
+  bool qr_taken = false;
+  for (int it = 0; it < 5; ++it) {
+    WCK(cgemm(adj(cmat<T>(cur, m, k, k, 1)), cmat<T>(cur, m, k, k, 1), cout_<T>(S, k, k, k, 1), T(1), T(0), B.gemm,
+              st));
+    *ortho_flops += 8.0 * k * k * m;
+    k_defect<T><<<1, 256, 0, st>>>(S, k, B.d_scalar);
+    WCK(cudaMemcpyAsync(hs, B.d_scalar, sizeof(double), cudaMemcpyDeviceToHost, st));
+    WCK(cudaStreamSynchronize(st));
+    const double fro = hs[0];
+    if (!(fro == fro)) return fail(MPS_ERR_NUMERIC, "non-finite value in a wide split");
+    if (it == 0 && fro > 0.1) {
+      qr_taken = true;
+      break;
+    }
+    WCK(cudaMemcpyAsync(nxt, cur, (size_t)m * k * sizeof(cx<T>), cudaMemcpyDeviceToDevice, st));
+    WCK(cgemm(cmat<T>(cur, m, k, k, 1), cmat<T>(S, k, k, k, 1), cout_<T>(nxt, m, k, k, 1), T(-0.5), T(1.5), B.gemm,
+              st));
+    *ortho_flops += 8.0 * k * k * m;
+    std::swap(cur, nxt);
+    if (fro < ns_stop) break;
+  }
+  if (qr_taken) {
+    // degenerate cluster: Householder QR, then (when vectors were completed
+    // from rounding noise) one subspace step with X and a second QR
+    const int grid = coop_grid(sizeof(T) == 8 ? 0 : 1, 1);
+    for (int pass = 0; pass < 2; ++pass) {
+      WCK(launch_wide_qr_t<T>(cmat<T>(cur, m, k, k, 1), cout_<T>(nxt, m, k, k, 1), 0, B.R, B.qr_work, B.d_err, grid,
+                              st));
+      std::swap(cur, nxt);
+      if (pass == 1 || k >= m || !subspace) break;
+      cx<T>* Y = reinterpret_cast<cx<T>*>(B.Y);
+      WCK(cgemm(adj(X), cmat<T>(cur, m, k, k, 1), cout_<T>(Y, nn, k, k, 1), T(1), T(0), B.gemm, st));
+      WCK(cgemm(X, cmat<T>(Y, nn, k, k, 1), cout_<T>(nxt, m, k, k, 1), T(1), T(0), B.gemm, st));
+      T* inv = reinterpret_cast<T*>(B.scal) + 2 * B.m;
+      k_colnorm<T><<<(k + 255) / 256, 256, 0, st>>>(nxt, m, k, cur, k, inv);
+      k_colscale<T><<<blocks_for((int64_t)m * k), 256, 0, st>>>(nxt, m, k, inv);
+      std::swap(cur, nxt);
+      *ortho_flops += 16.0 * m * nn * k;
+    }
+    int herr = 0;
+    WCK(cudaMemcpy(&herr, B.d_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (herr) return fail(MPS_ERR_TIMEOUT, "cooperative QR gave up at a grid barrier");
+  }
+  *result = cur;
+  return MPS_OK;
+}
+
+template <typename T>
+static int wide_gate2(mps_prog* p, WideBufs& B, cudaStream_t st, const DevOp& op) {
+  const int lo = op.site;
+  const int dl = p->hbond[lo], dm = p->hbond[lo + 1], dr = p->hbond[lo + 2];
+  cx<T>* sites = reinterpret_cast<cx<T>*>(p->d_sites);
+  cx<T>* A = sites + p->off[lo];
+  cx<T>* Bs = sites + p->off[lo + 1];
+  const int R = 2 * dl, Cc = 2 * dr;
+  cx<T>* theta = reinterpret_cast<cx<T>*>(B.theta);
+  cx<T>* tb = reinterpret_cast<cx<T>*>(B.tbuf);
+  WCK(cgemm(cmat<T>(A, R, dm, dm, 1), cmat<T>(Bs, dm, Cc, Cc, 1), cout_<T>(tb, R, Cc, Cc, 1), T(1), T(0), B.gemm,
+            st));
+  G16 g;
+  std::memcpy(g.m, op.m, sizeof(g.m));
+  k_theta_gate<T><<<blocks_for((int64_t)dl * dr), 256, 0, st>>>(tb, theta, dl, dr, g);
+  bool tr;
+  if (op.orient == ORIENT_TO_HI)
+    tr = false;
+  else if (op.orient == ORIENT_TO_LO)
+    tr = true;
+  else
+    tr = R > Cc;
+  const int m = tr ? Cc : R, nn = tr ? R : Cc, mm = std::min(R, Cc);
+  const CMat<T> X = tr ? cmat<T>(theta, Cc, R, 1, Cc) : cmat<T>(theta, R, Cc, Cc, 1);
+  cx<T>* G = reinterpret_cast<cx<T>*>(B.gram);
+  WCK(cgemm(X, adj(X), cout_<T>(G, m, m, m, 1), T(1), T(0), B.gemm, st));
+  const int kcap = std::min(p->chi_cap, mm);
+  WideEigArgs ea;
+  ea.G = G;
+  ea.W = B.W;
+  ea.lam = B.lam;
+  ea.m = m;
+  ea.mm = mm;
+  ea.kcap = kcap;
+  ea.mode = p->mode;
+  ea.cutoff = p->cutoff;
+  ea.work = B.eig_work;
+  ea.status = B.d_status;
+  const int prec = sizeof(T) == 8 ? 0 : 1;
+  WCK(launch_wide_eig(prec, ea, coop_grid(prec, 0), st));
+  WideEigStatus* hst = reinterpret_cast<WideEigStatus*>(B.h_pinned);
+  int* hbar = reinterpret_cast<int*>(B.h_pinned + 64);
+  WCK(cudaMemcpyAsync(hst, B.d_status, sizeof(WideEigStatus), cudaMemcpyDeviceToHost, st));
+  WCK(cudaMemcpyAsync(hbar, B.eig_work, 16, cudaMemcpyDeviceToHost, st));
+  WCK(cudaStreamSynchronize(st));
+  if (hbar[2]) return fail(MPS_ERR_TIMEOUT, "cooperative eigensolver gave up at a grid barrier");
+  if (hst->err & ERR_NAN) return fail(MPS_ERR_NUMERIC, "non-finite value in a wide split");
+  const int k = hst->k;
+  if (k < 1 || k > kcap) return fail(MPS_ERR_NUMERIC, "wide split returned an invalid bond dimension");
+  // W (m x k, ld kcap) -> compact (ld k) in W2, [subspace step], orthonormalise
+  cx<T>* Wk = reinterpret_cast<cx<T>*>(B.W2);
+  WCK(cudaMemcpy2DAsync(Wk, (size_t)k * sizeof(cx<T>), B.W, (size_t)kcap * sizeof(cx<T>), (size_t)k * sizeof(cx<T>),
+                        m, cudaMemcpyDeviceToDevice, st));
+  double extra = 0.0;
+  const bool fp32 = sizeof(T) == 4;
+  if (fp32 && k < m) {
+    cx<T>* Y = reinterpret_cast<cx<T>*>(B.Y);
+    cx<T>* W3 = reinterpret_cast<cx<T>*>(B.W3);
+    WCK(cgemm(adj(X), cmat<T>(Wk, m, k, k, 1), cout_<T>(Y, nn, k, k, 1), T(1), T(0), B.gemm, st));
+    WCK(cgemm(X, cmat<T>(Y, nn, k, k, 1), cout_<T>(W3, m, k, k, 1), T(1), T(0), B.gemm, st));
+    T* inv = reinterpret_cast<T*>(B.scal) + 2 * B.m;
+    k_colnorm<T><<<(k + 255) / 256, 256, 0, st>>>(W3, m, k, Wk, k, inv);
+    k_colscale<T><<<blocks_for((int64_t)m * k), 256, 0, st>>>(W3, m, k, inv);
+    extra += 16.0 * m * nn * k;
+    Wk = W3;
+  }
+  cx<T>* Wf = nullptr;
+  int rc = orthonormalize_w<T>(B, X, m, nn, k, Wk, true, st, &Wf, &extra);
+  if (rc) return rc;
+  T* iso = reinterpret_cast<T*>(B.scal);
+  T* oth = iso + B.m;
+  k_split_scales<T><<<(k + 255) / 256, 256, 0, st>>>(B.lam, B.d_status, op.orient == ORIENT_SQRT ? 1 : 0,
+                                                     (p->flags & MPS_FLAG_RENORM) ? 1 : 0, iso, oth);
+  cx<T>* Wo = reinterpret_cast<cx<T>*>(Wf == B.W2 ? B.W3 : B.W2);
+  if (Wo == Wf) Wo = reinterpret_cast<cx<T>*>(B.Y);
+  if (!tr) {
+    k_write_iso<T><<<blocks_for((int64_t)m * k), 256, 0, st>>>(Wf, m, k, iso, oth, 0, A, Wo);
+    WCK(cgemm(adj(cmat<T>(Wo, m, k, k, 1)), X, cout_<T>(Bs, k, Cc, Cc, 1), T(1), T(0), B.gemm, st));
+  } else {
+    k_write_iso<T><<<blocks_for((int64_t)m * k), 256, 0, st>>>(Wf, m, k, iso, oth, 1, Bs, Wo);
+    WCK(cgemm(cmat<T>(theta, R, Cc, Cc, 1), cmat<T>(Wo, Cc, k, k, 1, 1), cout_<T>(A, R, k, k, 1), T(1), T(0),
+              B.gemm, st));
+  }
+  const double flops = 32.0 * dl * dm * dr + 128.0 * dl * dr + 8.0 * m * m * nn + 8.0 * k * nn * m + extra;
+  const double eig_flops = (32.0 / 3.0) * m * m * m + 8.0 * m * m * k;
+  k_wide_commit<<<1, 1, 0, st>>>(p->d_stats, p->d_bond, lo + 1, B.d_status, flops, eig_flops);
+  WCK(cudaGetLastError());
+  p->hbond[lo + 1] = k;
+  return MPS_OK;
+}
+
+// Centre moves.  Right: A_c (2dl x dr) = Q R, A_{c+1} <- R A_{c+1}.  Left:
+// A_c^H (2dr x dl) = Q R, A_c <- Q^H, A_{c-1} <- A_{c-1} R^H.
+template <typename T>
+static int wide_move(mps_prog* p, WideBufs& B, cudaStream_t st, const DevOp& op) {
+  const int c = op.site;
+  cx<T>* sites = reinterpret_cast<cx<T>*>(p->d_sites);
+  const int prec = sizeof(T) == 8 ? 0 : 1;
+  const int grid = coop_grid(prec, 1);
+  cx<T>* tmp = reinterpret_cast<cx<T>*>(B.tbuf);
+  cx<T>* Rm = reinterpret_cast<cx<T>*>(B.R);
+  if (op.kind == OP_MOVE_R) {
+    const int dl = p->hbond[c], dr = p->hbond[c + 1], d2 = p->hbond[c + 2];
+    const int mr = 2 * dl, k = std::min(mr, dr);
+    cx<T>* Ac = sites + p->off[c];
+    cx<T>* An = sites + p->off[c + 1];
+    WCK(launch_wide_qr_t<T>(cmat<T>(Ac, mr, dr, dr, 1), cout_<T>(Ac, mr, k, k, 1), 0, Rm, B.qr_work, B.d_err, grid,
+                            st));
+    WCK(cgemm(cmat<T>(Rm, k, dr, dr, 1), cmat<T>(An, dr, 2 * d2, 2 * d2, 1), cout_<T>(tmp, k, 2 * d2, 2 * d2, 1),
+              T(1), T(0), B.gemm, st));
+    WCK(cudaMemcpyAsync(An, tmp, (size_t)k * 2 * d2 * sizeof(cx<T>), cudaMemcpyDeviceToDevice, st));
+    k_set_bond<<<1, 1, 0, st>>>(p->d_stats, p->d_bond, c + 1, k, 8.0 * k * dr * 2 * d2);
+    p->hbond[c + 1] = k;
+  } else {
+    const int dl = p->hbond[c], dr = p->hbond[c + 1], d0 = p->hbond[c - 1];
+    const int mr = 2 * dr, k = std::min(mr, dl);
+    cx<T>* Ac = sites + p->off[c];
+    cx<T>* Ap = sites + p->off[c - 1];
+    // M = A_c^H: M(i, j) = conj(A_c[j][i]) with A_c as dl x 2dr
+    WCK(launch_wide_qr_t<T>(cmat<T>(Ac, mr, dl, 1, mr, 1), cout_<T>(Ac, mr, k, 1, mr), 1, Rm, B.qr_work, B.d_err,
+                            grid, st));
+    WCK(cgemm(cmat<T>(Ap, 2 * d0, dl, dl, 1), adj(cmat<T>(Rm, k, dl, dl, 1)), cout_<T>(tmp, 2 * d0, k, k, 1), T(1),
+              T(0), B.gemm, st));
+    WCK(cudaMemcpyAsync(Ap, tmp, (size_t)2 * d0 * k * sizeof(cx<T>), cudaMemcpyDeviceToDevice, st));
+    k_set_bond<<<1, 1, 0, st>>>(p->d_stats, p->d_bond, c, k, 8.0 * k * dl * 2 * d0);
+    p->hbond[c] = k;
+  }
+  WCK(cudaGetLastError());
+  return MPS_OK;
+}
+
+template <typename T>
+static int wide_run_t(mps_prog* p, WideBufs& B, cudaStream_t st, const std::vector<DevOp>& ops) {
+  cx<T>* sites = reinterpret_cast<cx<T>*>(p->d_sites);
+  for (const DevOp& op : ops) {
+    int rc = MPS_OK;
+    if (op.kind == OP_GATE1) {
+      G16 g;
+      std::memcpy(g.m, op.m, sizeof(g.m));
+      const int dl = p->hbond[op.site], dr = p->hbond[op.site + 1];
+      k_wide_gate1<T><<<blocks_for((int64_t)dl * dr), 256, 0, st>>>(sites + p->off[op.site], dl, dr, g);
+      k_set_bond<<<1, 1, 0, st>>>(p->d_stats, p->d_bond, -1, 0, 0.0);
+      WCK(cudaGetLastError());
+    } else if (op.kind == OP_GATE2) {
+      rc = wide_gate2<T>(p, B, st, op);
+    } else {
+      rc = wide_move<T>(p, B, st, op);
+    }
+    if (rc) return rc;
+  }
+  return MPS_OK;
+}
+
+bool prog_is_wide(const mps_prog* p) { return p->chi_cap > kChiLimit; }
+
+int wide_run(mps_ctx* c, Lane& L, mps_prog* p) {
+  std::vector<DevOp> ops;
+  compile_program(p, ops);
+  WideBufs* B = nullptr;
+  int rc = wide_bufs(c, p->prec, p->chi_cap, &B);
+  if (rc) return rc;
+  rc = p->prec == MPS_PREC_FP64 ? wide_run_t<double>(p, *B, L.stream, ops) : wide_run_t<float>(p, *B, L.stream, ops);
+  if (rc) return rc;
+  WCK(cudaEventRecord(p->ev, L.stream));
+  p->submitted = true;
+  return MPS_OK;
+}
+
+// ------------------------------------------------------------ measurement
+template <typename T>
+static int wide_expect_t(mps_prog* p, WideBufs& B, cudaStream_t st, const uint8_t* codes, int n_terms, double* out) {
+  cx<T>* sites = reinterpret_cast<cx<T>*>(p->d_sites);
+  cx<T>* E = reinterpret_cast<cx<T>*>(B.gram);
+  cx<T>* F = reinterpret_cast<cx<T>*>(B.theta);
+  cx<T>* H = reinterpret_cast<cx<T>*>(B.tbuf);
+  double* d_out = nullptr;
+  WCK(cudaMalloc(&d_out, 2 * sizeof(double) * (size_t)std::max(1, n_terms)));
+  const cx<T> one = mk<T>(T(1), T(0));
+  for (int t = 0; t < n_terms; ++t) {
+    WCK(cudaMemcpyAsync(E, &one, sizeof(one), cudaMemcpyHostToDevice, st));
+    for (int i = 0; i < p->n; ++i) {
+      const int dl = p->hbond[i], dr = p->hbond[i + 1];
+      const cx<T>* Ai = sites + p->off[i];
+      WCK(cgemm(cmat<T>(E, dl, dl, dl, 1), cmat<T>(Ai, dl, 2 * dr, 2 * dr, 1), cout_<T>(F, dl, 2 * dr, 2 * dr, 1),
+                T(1), T(0), B.gemm, st));
+      const int code = codes[(size_t)t * p->n + i];
+      const cx<T>* Hs = F;
+      if (code != 0) {
+        k_pauli<T><<<blocks_for((int64_t)dl * dr), 256, 0, st>>>(F, H, dl, dr, code);
+        Hs = H;
+      }
+      WCK(cgemm(adj(cmat<T>(Ai, 2 * dl, dr, dr, 1)), cmat<T>(Hs, 2 * dl, dr, dr, 1), cout_<T>(E, dr, dr, dr, 1), T(1),
+                T(0), B.gemm, st));
+    }
+    k_store_scalar<T><<<1, 1, 0, st>>>(E, d_out + 2 * t);
+  }
+  cudaError_t e = cudaMemcpyAsync(out, d_out, 2 * sizeof(double) * n_terms, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  cudaFree(d_out);
+  if (e != cudaSuccess) return fail(MPS_ERR_CUDA, cudaGetErrorString(e));
+  return MPS_OK;
+}
+
+int wide_expect(mps_prog* p, const uint8_t* codes, int n_terms, double* out) {
+  WideBufs* B = nullptr;
+  int rc = wide_bufs(p->ctx, p->prec, p->chi_cap, &B);
+  if (rc) return rc;
+  cudaStream_t st = p->ctx->lane0.stream;
+  return p->prec == MPS_PREC_FP64 ? wide_expect_t<double>(p, *B, st, codes, n_terms, out)
+                                  : wide_expect_t<float>(p, *B, st, codes, n_terms, out);
+}
+
+template <typename T>
+static int wide_sample_t(mps_prog* p, WideBufs& B, cudaStream_t st, int shots, uint64_t seed, uint8_t* h_bits) {
+  const int n = p->n;
+  cx<T>* sites = reinterpret_cast<cx<T>*>(p->d_sites);
+  std::vector<int64_t> eoff(n + 2, 0);
+  int64_t tot = 0;
+  for (int i = 1; i <= n; ++i) {
+    eoff[i] = tot;
+    tot += (int64_t)p->hbond[i] * p->hbond[i];
+  }
+  int maxd = 1;
+  for (int i = 0; i <= n; ++i) maxd = std::max(maxd, p->hbond[i]);
+  const size_t eb = sizeof(cx<T>);
+  const size_t vbytes = (size_t)shots * maxd * eb, ubytes = (size_t)shots * 2 * maxd * eb;
+  char* buf = nullptr;
+  WCK(cudaMalloc(&buf, (size_t)tot * eb + vbytes + 2 * ubytes + (size_t)shots * n + 1024));
+  cx<T>* env = reinterpret_cast<cx<T>*>(buf);
+  cx<T>* V = reinterpret_cast<cx<T>*>(buf + (size_t)tot * eb);
+  cx<T>* U = reinterpret_cast<cx<T>*>(buf + (size_t)tot * eb + vbytes);
+  cx<T>* Q = reinterpret_cast<cx<T>*>(buf + (size_t)tot * eb + vbytes + ubytes);
+  uint8_t* d_bits = reinterpret_cast<uint8_t*>(buf + (size_t)tot * eb + vbytes + 2 * ubytes);
+  cx<T>* F = reinterpret_cast<cx<T>*>(B.theta);
+  int rc = MPS_OK;
+  auto run = [&]() -> int {
+    // right environments: R_n = 1, R_i = sum_s A_i[:, s, :] R_{i+1} A_i[:, s, :]^H
+    const cx<T> one = mk<T>(T(1), T(0));
+    WCK(cudaMemcpyAsync(env + eoff[n], &one, sizeof(one), cudaMemcpyHostToDevice, st));
+    for (int i = n - 1; i >= 1; --i) {
+      const int dl = p->hbond[i], dr = p->hbond[i + 1];
+      const cx<T>* Ai = sites + p->off[i];
+      WCK(cgemm(cmat<T>(Ai, 2 * dl, dr, dr, 1), cmat<T>(env + eoff[i + 1], dr, dr, dr, 1),
+                cout_<T>(F, 2 * dl, dr, dr, 1), T(1), T(0), B.gemm, st));
+      WCK(cgemm(cmat<T>(F, dl, 2 * dr, 2 * dr, 1), adj(cmat<T>(Ai, dl, 2 * dr, 2 * dr, 1)),
+                cout_<T>(env + eoff[i], dl, dl, dl, 1), T(1), T(0), B.gemm, st));
+    }
+    // shots: V (S x dl) starts at 1
+    std::vector<cx<T>> ones((size_t)shots, one);
+    WCK(cudaMemcpyAsync(V, ones.data(), (size_t)shots * eb, cudaMemcpyHostToDevice, st));
+    for (int i = 0; i < n; ++i) {
+      const int dl = p->hbond[i], dr = p->hbond[i + 1];
+      const cx<T>* Ai = sites + p->off[i];
+      WCK(cgemm(cmat<T>(V, shots, dl, dl, 1), cmat<T>(Ai, dl, 2 * dr, 2 * dr, 1), cout_<T>(U, shots, 2 * dr, 2 * dr, 1),
+                T(1), T(0), B.gemm, st));
+      const cx<T>* Rn = i + 1 < n ? env + eoff[i + 1] : nullptr;
+      if (Rn)
+        WCK(cgemm(cmat<T>(U, 2 * shots, dr, dr, 1), cmat<T>(Rn, dr, dr, dr, 1), cout_<T>(Q, 2 * shots, dr, dr, 1),
+                  T(1), T(0), B.gemm, st));
+      else
+        WCK(cudaMemcpyAsync(Q, U, (size_t)shots * 2 * dr * eb, cudaMemcpyDeviceToDevice, st));
+      k_wide_sample_step<T><<<(shots * 32 + 255) / 256, 256, 0, st>>>(U, Q, V, shots, dr, i, n, seed, d_bits);
+      WCK(cudaGetLastError());
+    }
+    WCK(cudaMemcpyAsync(h_bits, d_bits, (size_t)shots * n, cudaMemcpyDeviceToHost, st));
+    WCK(cudaStreamSynchronize(st));
+    return MPS_OK;
+  };
+  rc = run();
+  cudaFree(buf);
+  return rc;
+}
+
+int wide_sample(mps_prog* p, int shots, uint64_t seed, uint8_t* h_all_bits) {
+  WideBufs* B = nullptr;
+  int rc = wide_bufs(p->ctx, p->prec, p->chi_cap, &B);
+  if (rc) return rc;
+  cudaStream_t st = p->ctx->lane0.stream;
+  return p->prec == MPS_PREC_FP64 ? wide_sample_t<double>(p, *B, st, shots, seed, h_all_bits)
+                                  : wide_sample_t<float>(p, *B, st, shots, seed, h_all_bits);
+}
+
+template <typename T>
+static int wide_amp_one_t(mps_prog* p, WideBufs& B, cudaStream_t st, const int* bits, double* out) {
+  cx<T>* sites = reinterpret_cast<cx<T>*>(p->d_sites);
+  cx<T>* v0 = reinterpret_cast<cx<T>*>(B.theta);
+  cx<T>* v1 = reinterpret_cast<cx<T>*>(B.tbuf);
+  const cx<T> one = mk<T>(T(1), T(0));
+  WCK(cudaMemcpyAsync(v0, &one, sizeof(one), cudaMemcpyHostToDevice, st));
+  for (int i = 0; i < p->n; ++i) {
+    const int dl = p->hbond[i], dr = p->hbond[i + 1];
+    const cx<T>* Ai = sites + p->off[i] + (int64_t)bits[i] * dr;
+    WCK(cgemm(cmat<T>(v0, 1, dl, dl, 1), cmat<T>(Ai, dl, dr, 2 * dr, 1), cout_<T>(v1, 1, dr, dr, 1), T(1), T(0),
+              B.gemm, st));
+    std::swap(v0, v1);
+  }
+  double* d = reinterpret_cast<double*>(B.d_scalar);
+  k_store_scalar<T><<<1, 1, 0, st>>>(v0, d);
+  WCK(cudaMemcpyAsync(out, d, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  WCK(cudaStreamSynchronize(st));
+  return MPS_OK;
+}
+
+int wide_amp_one(mps_prog* p, const int* bits, double* out) {
+  WideBufs* B = nullptr;
+  int rc = wide_bufs(p->ctx, p->prec, p->chi_cap, &B);
+  if (rc) return rc;
+  cudaStream_t st = p->ctx->lane0.stream;
+  return p->prec == MPS_PREC_FP64 ? wide_amp_one_t<double>(p, *B, st, bits, out)
+                                  : wide_amp_one_t<float>(p, *B, st, bits, out);
+}
+
+int wide_gemm_counts(mps_ctx* c, int* tc, int* simt) {
+  *tc = *simt = 0;
+  if (!c->wide) return MPS_OK;
+  for (auto& b : reinterpret_cast<WideAll*>(c->wide)->b) {
+    *tc += b.gemm.tc_launches;
+    *simt += b.gemm.simt_launches;
+  }
+  return MPS_OK;
+}
+
+// Cross-check entry of the tensor-core GEMM against the CUDA-core kernel.
+int wide_diag_cgemm(mps_ctx* c, int M, int N, int K, const double* a, const double* b, double* out_tc,
+                    double* out_simt) {
+  WideBufs* B = nullptr;
+  const int chi = std::max(std::max(M, N), std::max(K, 64));
+  int rc = wide_bufs(c, MPS_PREC_FP32, (chi + 1) / 2 + 64, &B);
+  if (rc) return rc;
+  cudaStream_t st = c->lane0.stream;
+  std::vector<cx<float>> ha((size_t)M * K), hb((size_t)K * N), hc((size_t)M * N);
+  for (size_t i = 0; i < ha.size(); ++i) ha[i] = mk<float>((float)a[2 * i], (float)a[2 * i + 1]);
+  for (size_t i = 0; i < hb.size(); ++i) hb[i] = mk<float>((float)b[2 * i], (float)b[2 * i + 1]);
+  cx<float>* da = reinterpret_cast<cx<float>*>(B->theta);
+  cx<float>* db = reinterpret_cast<cx<float>*>(B->tbuf);
+  cx<float>* dc = reinterpret_cast<cx<float>*>(B->gram);
+  WCK(cudaMemcpyAsync(da, ha.data(), ha.size() * 8, cudaMemcpyHostToDevice, st));
+  WCK(cudaMemcpyAsync(db, hb.data(), hb.size() * 8, cudaMemcpyHostToDevice, st));
+  for (int pass = 0; pass < 2; ++pass) {
+    if (pass == 0)
+      WCK(cgemm(cmat<float>(da, M, K, K, 1), cmat<float>(db, K, N, N, 1), cout_<float>(dc, M, N, N, 1), 1.0f, 0.0f,
+                B->gemm, st));
+    else
+      WCK(cgemm_simt(cmat<float>(da, M, K, K, 1), cmat<float>(db, K, N, N, 1), cout_<float>(dc, M, N, N, 1), 1.0f,
+                     0.0f, st));
+    WCK(cudaMemcpyAsync(hc.data(), dc, hc.size() * 8, cudaMemcpyDeviceToHost, st));
+    WCK(cudaStreamSynchronize(st));
+    double* o = pass == 0 ? out_tc : out_simt;
+    for (size_t i = 0; i < hc.size(); ++i) {
+      o[2 * i] = hc[i].re;
+      o[2 * i + 1] = hc[i].im;
+    }
+  }
+  int herr = 0;
+  WCK(cudaMemcpy(&herr, B->gemm.d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (herr) return fail(MPS_ERR_TIMEOUT, "tensor-core GEMM wait timed out");
+  return MPS_OK;
+}
+
+}  // namespace gbmps

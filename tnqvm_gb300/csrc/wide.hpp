@@ -1,0 +1,128 @@
+// Wide two-site path: bond dimensions above the single-CTA limit (up to
+// kWideChi).  Host-driven per gate: complex GEMMs (tcgen05 for complex64,
+// CUDA cores for complex128), a cooperative (grid-wide) tridiagonal
+// eigensolver and a cooperative Householder QR.  Declarations shared by
+// k_gemm.cu, k_coop.cu and wide.cu.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "mps_common.cuh"
+
+namespace gbmps {
+
+constexpr int kWideChi = 1024;          // largest bond of the wide path
+constexpr int kWideM = 2 * kWideChi;    // largest Gram / theta side
+
+// Strided complex matrix: element (i, j) is p[i * rs + j * cs], conjugated
+// when conj != 0.
+template <typename T>
+struct CMat {
+  const cx<T>* p;
+  int64_t rs, cs;
+  int rows, cols;
+  int conj;
+};
+template <typename T>
+struct CMatOut {
+  cx<T>* p;
+  int64_t rs, cs;
+  int rows, cols;
+};
+
+template <typename T>
+inline CMat<T> cmat(const void* p, int rows, int cols, int64_t rs, int64_t cs, int conj = 0) {
+  CMat<T> v;
+  v.p = reinterpret_cast<const cx<T>*>(p);
+  v.rs = rs;
+  v.cs = cs;
+  v.rows = rows;
+  v.cols = cols;
+  v.conj = conj;
+  return v;
+}
+// The conjugate transpose of a view.
+template <typename T>
+inline CMat<T> adj(CMat<T> v) {
+  CMat<T> r = v;
+  r.rs = v.cs;
+  r.cs = v.rs;
+  r.rows = v.cols;
+  r.cols = v.rows;
+  r.conj = !v.conj;
+  return r;
+}
+template <typename T>
+inline CMatOut<T> cout_(void* p, int rows, int cols, int64_t rs, int64_t cs) {
+  CMatOut<T> v;
+  v.p = reinterpret_cast<cx<T>*>(p);
+  v.rs = rs;
+  v.cs = cs;
+  v.rows = rows;
+  v.cols = cols;
+  return v;
+}
+
+// Device workspace of the GEMMs: the split (hi/lo) real-embedded operands of
+// the tensor-core path.  Sized for the largest wide product.
+struct GemmWs {
+  float* a_hi = nullptr;
+  float* a_lo = nullptr;
+  float* b_hi = nullptr;
+  float* b_lo = nullptr;
+  size_t a_elems = 0, b_elems = 0;
+  int* d_err = nullptr;  // barrier/wait time-outs of the tensor-core kernel
+  int tc_launches = 0;   // tensor-core GEMM launches issued (diagnostics)
+  int simt_launches = 0;
+};
+int gemm_ws_init(GemmWs& ws, size_t a_elems, size_t b_elems);
+void gemm_ws_free(GemmWs& ws);
+
+// C = alpha * A * B + beta * C with A (M x K), B (K x N), C (M x N) views.
+// complex64 runs on tcgen05 (3xTF32: hi*hi + hi*lo + lo*hi, FP32
+// accumulation in tensor memory) when the product fills at least one
+// 128 x 64 tile, else on CUDA cores; complex128 runs on CUDA cores.
+cudaError_t cgemm(const CMat<float>& A, const CMat<float>& B, const CMatOut<float>& C, float alpha, float beta,
+                  GemmWs& ws, cudaStream_t st);
+cudaError_t cgemm(const CMat<double>& A, const CMat<double>& B, const CMatOut<double>& C, double alpha,
+                  double beta, GemmWs& ws, cudaStream_t st);
+// Force the CUDA-core kernel (cross-checks of the tensor-core path).
+cudaError_t cgemm_simt(const CMat<float>& A, const CMat<float>& B, const CMatOut<float>& C, float alpha,
+                       float beta, cudaStream_t st);
+
+// ------------------------------------------------------------ cooperative
+// Result of one wide eigen-decomposition (device struct, read back by the host).
+struct WideEigStatus {
+  int32_t k;        // kept dimension
+  int32_t err;      // ERR_* bits, plus kCoopTimeout
+  double total;     // sum of the (clamped) eigenvalues
+  double kept;      // sum of the kept ones
+  double lam_max;
+};
+constexpr int32_t kCoopTimeout = 1 << 8;
+
+struct WideEigArgs {
+  void* G;          // m x m Hermitian (row-major, ld m), destroyed (holds the reflectors)
+  void* W;          // out: m x kcap kept eigenvectors (row-major, ld kcap)
+  double* lam;      // out: m eigenvalues, descending
+  int m;
+  int mm;           // singular values of the split (min side of theta); the keep rule reads lam[0..mm)
+  int kcap;         // largest k allowed (chi cap); the keep rule picks k <= kcap
+  int mode;         // TRUNC_EXATN / TRUNC_ITENSOR
+  double cutoff;
+  void* work;       // cooperative scratch (wide_eig_work_bytes)
+  WideEigStatus* status;
+};
+size_t wide_eig_work_bytes(int prec, int m);
+cudaError_t launch_wide_eig(int prec, const WideEigArgs& a, int grid, cudaStream_t st);
+
+// Householder QR of the view M (mr x nc): Q (mr x k, k = min(mr, nc)) is
+// written through the view Q (conjugated when qconj), R (k x nc) row-major to
+// R.  The input is copied to the work buffer first, so Q may alias M.
+size_t wide_qr_work_bytes(int prec, int mr, int nc);
+template <typename T>
+cudaError_t launch_wide_qr_t(const CMat<T>& M, const CMatOut<T>& Q, int qconj, void* R, void* work, int* err,
+                             int grid, cudaStream_t st);
+int coop_grid(int prec, int which);  // co-resident grid of the cooperative kernels (0 eig, 1 qr)
+
+}  // namespace gbmps

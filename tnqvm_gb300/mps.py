@@ -18,6 +18,7 @@ TRUNC_EXATN, TRUNC_ITENSOR = 0, 1
 PREC_FP64, PREC_FP32 = 0, 1
 FLAG_RENORM, FLAG_PER_GATE = 1, 2
 CHI_LIMIT = 64
+WIDE_CHI_LIMIT = 1024
 
 _ERR_NAMES = {1: "MPS_ERR_ARG", 2: "MPS_ERR_OOM", 3: "MPS_ERR_TIMEOUT", 4: "MPS_ERR_NUMERIC",
               5: "MPS_ERR_CUDA", 6: "MPS_ERR_STATE", 7: "MPS_ERR_UNSUPPORTED"}
@@ -72,6 +73,8 @@ SIGNATURES = [
     ("mps_gates", _c.c_int, [_P, _c.c_int, _c.POINTER(_c.c_int32), _c.POINTER(_c.c_int32), _DP]),
     ("mps_gate2_apply_noalloc", _c.c_int, [_c.c_int, _c.c_int, _c.c_int, _c.c_double, _P, _c.c_int64,
                                             _P, _c.POINTER(_c.c_int), _DP, _P]),
+    ("mps_diag_cgemm", _c.c_int, [_P, _c.c_int, _c.c_int, _c.c_int, _DP, _DP, _DP, _DP]),
+    ("mps_diag_gemm_counts", _c.c_int, [_P, _c.POINTER(_c.c_int), _c.POINTER(_c.c_int)]),
 ]
 
 GATE_IDS = {name: i for i, name in enumerate(
@@ -198,6 +201,26 @@ class Context:
     def serve_stop(self):
         _check(_lib.mps_serve_stop(self.h))
         self.serving = False
+
+    # ---- diagnostics of the wide path
+    def diag_cgemm(self, a, b):
+        """complex64 product a @ b on the tensor-core and on the CUDA-core
+        kernel; returns (c_tc, c_simt) as complex128 arrays."""
+        a = np.ascontiguousarray(a, dtype=np.complex128)
+        b = np.ascontiguousarray(b, dtype=np.complex128)
+        M, K = a.shape
+        N = b.shape[1]
+        ct = np.zeros((M, N), dtype=np.complex128)
+        cs = np.zeros((M, N), dtype=np.complex128)
+        _check(_lib.mps_diag_cgemm(self.h, M, N, K, _dptr(a.view(np.float64)), _dptr(b.view(np.float64)),
+                                   _dptr(ct.view(np.float64)), _dptr(cs.view(np.float64))))
+        return ct, cs
+
+    def gemm_counts(self):
+        """(tensor-core, CUDA-core) GEMM launches of the wide path so far."""
+        t, s = ctypes.c_int(), ctypes.c_int()
+        _check(_lib.mps_diag_gemm_counts(self.h, ctypes.byref(t), ctypes.byref(s)))
+        return t.value, s.value
 
 
 class Graph:
