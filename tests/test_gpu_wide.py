@@ -83,7 +83,7 @@ def test_wide_truncated_fp64_vs_oracle(ctx, mode, omode):
         tol = 1e-9 if mode == M.TRUNC_ITENSOR else 1e-8
         for s, v in zip(paulis, vals):
             assert abs(v - ref.expect_pauli(s)) < tol, s
-        assert abs(p.truncation_fidelity() - ref.fidelity) < 1e-9
+        assert abs(p.truncation_fidelity() - ref.fidelity) < tol
 
 
 @pytest.mark.parametrize("mode", [M.TRUNC_EXATN, M.TRUNC_ITENSOR])

@@ -272,7 +272,7 @@ __global__ void __launch_bounds__(kCoopThreads, 1) k_wide_eig(WideEigArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int m = a.m, G = gridDim.x, cta = blockIdx.x, tid = threadIdx.x, nt = blockDim.x;
   const int lane = tid & 31, warp = tid >> 5;
-  EigWork<T> wk = eig_work<T>(a.work, m, G);
+  EigWork<T> wk = eig_work<T>(a.work, m, a.grid0);
   cx<T>* A = reinterpret_cast<cx<T>*>(a.G);
   T* sd = reinterpret_cast<T*>(smem);
   T* se = sd + m;
@@ -289,7 +289,6 @@ __global__ void __launch_bounds__(kCoopThreads, 1) k_wide_eig(WideEigArgs a) {
   T* red = reinterpret_cast<T*>(redb);
   cx<T>* redc = reinterpret_cast<cx<T>*>(redb + 256);
   double* redd = reinterpret_cast<double*>(redb + 1024);
-  int* sint = reinterpret_cast<int*>(redb + 2048);
 
   // ---- 1. tridiagonalisation
   cx<T>* vprev = reinterpret_cast<cx<T>*>(uni);
@@ -495,56 +494,76 @@ __global__ void __launch_bounds__(kCoopThreads, 1) k_wide_eig(WideEigArgs a) {
   }
   if (!grid_sync(wk.bar)) return;
 
-  // ---- keep rule (CTA 0), broadcast k
-  if (cta == 0) {
-    double* dl = reinterpret_cast<double*>(uni);
-    for (int i = tid; i < m; i += nt) dl[i] = __ldcg(a.lam + i);
-    __syncthreads();
-    if (tid == 0) {
-      double total = 0.0;
-      int bad = 0;
-      for (int i = 0; i < a.mm; ++i) {
-        const double v = dl[i];
-        if (!(v == v) || isinf(v)) bad = 1;
-        total += v > 0.0 ? v : 0.0;
+  if (cta == 0 && tid == 0) a.status_err[0] = *(volatile int*)&wk.bar->err;
+}
+
+// Kept eigenvectors (phase 2 of the decomposition): columns 0..kv-1 of W
+// (row stride ld) are the eigenvectors of ranks 0..kv-1, from the
+// tridiagonal, ranks and reflectors that k_wide_eig left in G and the work
+// buffer.
+template <typename T>
+__global__ void __launch_bounds__(kCoopThreads, 1) k_wide_eigvec(WideEigArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int m = a.m, G = gridDim.x, cta = blockIdx.x, tid = threadIdx.x, nt = blockDim.x;
+  const int lane = tid & 31, warp = tid >> 5;
+  EigWork<T> wk = eig_work<T>(a.work, m, a.grid0);
+  const cx<T>* A = reinterpret_cast<const cx<T>*>(a.G);
+  T* sd = reinterpret_cast<T*>(smem);
+  T* se = sd + m;
+  int* sbs = reinterpret_cast<int*>(smem + al256(2 * m * sizeof(T)));
+  int* sbt = sbs + m;
+  unsigned char* uni = smem + al256(2 * m * sizeof(T)) + al256(2 * m * sizeof(int));
+  size_t usz = 3 * (size_t)m * sizeof(cx<T>);
+  {
+    const size_t wb = (size_t)m * CoopPrec<T>::cb * sizeof(cx<T>);
+    if (wb > usz) usz = wb;
+    if ((size_t)m * sizeof(double) > usz) usz = (size_t)m * sizeof(double);
+  }
+  unsigned char* redb = uni + al256(usz);
+  const T eps = T(CoopPrec<T>::eps);
+  for (int i = tid; i < m; i += nt) {
+    sd[i] = __ldcg(wk.td + i);
+    se[i] = __ldcg(wk.te + i);
+  }
+  __syncthreads();
+  if (tid == 0) {
+    int s0 = 0;
+    for (int i = 0; i < m; ++i) {
+      bool split = i == m - 1;
+      if (!split && fabs(se[i]) <= eps * (fabs(sd[i]) + fabs(sd[i + 1]))) {
+        split = true;
+        se[i] = T(0);
       }
-      int k = keep_rule(dl, a.mm, a.mode, a.cutoff, a.kcap);
-      if (k > a.kcap) k = a.kcap;
-      double kept = 0.0;
-      for (int i = 0; i < k; ++i) kept += dl[i] > 0.0 ? dl[i] : 0.0;
-      a.status->k = k;
-      a.status->total = total;
-      a.status->kept = kept;
-      a.status->lam_max = dl[0];
-      a.status->err = bad ? ERR_NAN : 0;
-      wk.bar->k = k;
+      if (split) {
+        for (int r = s0; r <= i; ++r) {
+          sbs[r] = s0;
+          sbt[r] = i;
+        }
+        s0 = i + 1;
+      }
     }
   }
-  if (!grid_sync(wk.bar)) return;
-  const int k = *(volatile int*)&wk.bar->k;
-
-  // ---- 4a. twisted vectors of the kept eigenvalues
+  __syncthreads();
+  const int k = a.kv;
+  // ---- twisted vectors of the kept eigenvalues
   cx<T>* W = reinterpret_cast<cx<T>*>(a.W);
   for (int c = cta * nt + tid; c < k; c += G * nt) {
     const int j = __ldcg(wk.perm + c);
-    coop_twisted<T>(W, m, a.kcap, c, __ldcg(wk.lamj + j), sbs[j], sbt[j], sd, se);
+    coop_twisted<T>(W, m, a.ld, c, __ldcg(wk.lamj + j), sbs[j], sbt[j], sd, se);
   }
   if (!grid_sync(wk.bar)) return;
 
-  // ---- 4b. back-transform W <- Q W, CB columns per CTA in shared memory
+  // ---- back-transform W <- Q W, CB columns per CTA in shared memory
   constexpr int CB = CoopPrec<T>::cb;
   constexpr int Q = kCoopThreads / CB;  // row chunks
   cx<T>* Ws = reinterpret_cast<cx<T>*>(uni);
-  cx<T>* sv = redc;  // Q x CB partial sums live after red (fits in 2 KB)
-  cx<T>* part = reinterpret_cast<cx<T>*>(redb + 1024);
-  (void)sv;
-  (void)sint;
+  cx<T>* part = reinterpret_cast<cx<T>*>(redb + 1024);  // per-warp partial sums (CB each)
   const int ngroups = (k + CB - 1) / CB;
   for (int g = cta; g < ngroups; g += G) {
     const int c0 = g * CB;
     for (int t = tid; t < m * CB; t += nt) {
       const int i = t / CB, c = t - i * CB;
-      Ws[t] = c0 + c < k ? ldcg(W + (int64_t)i * a.kcap + c0 + c) : mk<T>(T(0), T(0));
+      Ws[t] = c0 + c < k ? ldcg(W + (int64_t)i * a.ld + c0 + c) : mk<T>(T(0), T(0));
     }
     __syncthreads();
     const int c = tid % CB, q = tid / CB;
@@ -573,11 +592,11 @@ __global__ void __launch_bounds__(kCoopThreads, 1) k_wide_eig(WideEigArgs a) {
     }
     for (int t = tid; t < m * CB; t += nt) {
       const int i = t / CB, cc = t - i * CB;
-      if (c0 + cc < k) W[(int64_t)i * a.kcap + c0 + cc] = Ws[t];
+      if (c0 + cc < k) W[(int64_t)i * a.ld + c0 + cc] = Ws[t];
     }
     __syncthreads();
   }
-  if (cta == 0 && tid == 0) a.status->err |= *(volatile int*)&wk.bar->err;
+  if (cta == 0 && tid == 0) a.status_err[0] = *(volatile int*)&wk.bar->err;
 }
 
 // ------------------------------------------------------------------- QR
@@ -714,6 +733,7 @@ __global__ void __launch_bounds__(kCoopThreads, 1) k_wide_qr(QrArgsT<T> a) {
       if (lane == 0) stcg(y + j, ldcg(y + j) - tw);
       __syncwarp();
     }
+    __syncthreads();  // column j+1 is final before its owner forms the next reflector
   }
   if (!grid_sync(wk.bar)) return;
   // 2. R (k x nc): R[r][c] = MT[c][r] for r <= c
@@ -816,14 +836,19 @@ static cudaError_t eig_launch(const WideEigArgs& a, int grid, cudaStream_t st) {
     cudaError_t e = cudaFuncSetAttribute(k_wide_eig<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)eig_smem_bytes<T>(kWideM));
     if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(k_wide_eigvec<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)eig_smem_bytes<T>(kWideM));
+    if (e != cudaSuccess) return e;
     attr = true;
   }
   cudaError_t e = cudaMemsetAsync(a.work, 0, 256, st);
   if (e != cudaSuccess) return e;
   const size_t sm = eig_smem_bytes<T>(a.m);
   WideEigArgs arg = a;
+  arg.grid0 = grid;
   void* params[] = {&arg};
-  return cudaLaunchCooperativeKernel((const void*)k_wide_eig<T>, dim3(grid), dim3(kCoopThreads), params, sm, st);
+  const void* fn = a.phase == 0 ? (const void*)k_wide_eig<T> : (const void*)k_wide_eigvec<T>;
+  return cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(kCoopThreads), params, sm, st);
 }
 
 cudaError_t launch_wide_eig(int prec, const WideEigArgs& a, int grid, cudaStream_t st) {

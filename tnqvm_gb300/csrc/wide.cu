@@ -23,6 +23,7 @@
 
 #include "../../include/gb300mps.h"
 #include "engine_internal.hpp"
+#include "keep.cuh"
 #include "wide.hpp"
 
 namespace gbmps {
@@ -65,13 +66,10 @@ __global__ void k_wide_gate1(cx<T>* A, int dl, int dr, G16 g) {
 }
 
 // Split scales: exatn puts sqrt(S) on both sides, itensor leaves the
-// isometric side as is; renormalisation rescales the kept part to the
-// pre-truncation norm.
+// isometric side as is; rn rescales the kept part to the pre-truncation norm
+// (1 without renormalisation).
 template <typename T>
-__global__ void k_split_scales(const double* lam, const WideEigStatus* st, int sqrt_mode, int renorm, T* iso,
-                               T* oth) {
-  const int k = st->k;
-  const double rn = (renorm && st->kept > 0.0) ? sqrt(st->total / st->kept) : 1.0;
+__global__ void k_split_scales(const double* lam, int k, int sqrt_mode, double rn, T* iso, T* oth) {
   for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < k; j += gridDim.x * blockDim.x) {
     const double v = lam[j];
     const double sv = v > 0.0 ? sqrt(v) : 0.0;
@@ -127,30 +125,29 @@ __global__ void k_defect(const cx<T>* S, int k, double* out) {
 // Column normalisation of W2 (m x k, ld k); a vanished column takes the
 // column of Wf (ld ldf) instead.
 template <typename T>
-__global__ void k_colnorm(cx<T>* W2, int m, int k, const cx<T>* Wf, int ldf, T* inv) {
+__global__ void k_colnorm(cx<T>* W2, int m, int k, int ld, const cx<T>* Wf, int ldf, T* inv) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= k) return;
   T s2 = T(0);
-  for (int i = 0; i < m; ++i) s2 += abs2(W2[(int64_t)i * k + j]);
+  for (int i = 0; i < m; ++i) s2 += abs2(W2[(int64_t)i * ld + j]);
   const T tiny = sizeof(T) == 4 ? T(1e-36) : T(1e-280);
   inv[j] = s2 > tiny ? T(1) / sqrt(s2) : T(0);
   if (!(s2 > tiny))
-    for (int i = 0; i < m; ++i) W2[(int64_t)i * k + j] = Wf[(int64_t)i * ldf + j];
+    for (int i = 0; i < m; ++i) W2[(int64_t)i * ld + j] = Wf[(int64_t)i * ldf + j];
 }
 template <typename T>
-__global__ void k_colscale(cx<T>* W2, int m, int k, const T* inv) {
+__global__ void k_colscale(cx<T>* W2, int m, int k, int ld, const T* inv) {
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < (int64_t)m * k;
        t += (int64_t)gridDim.x * blockDim.x) {
-    const int j = (int)(t % k);
-    if (inv[j] > T(0)) W2[t] = scl(W2[t], inv[j]);
+    const int i = (int)(t / k), j = (int)(t - (int64_t)i * k);
+    if (inv[j] > T(0)) W2[(int64_t)i * ld + j] = scl(W2[(int64_t)i * ld + j], inv[j]);
   }
 }
 
 // Statistics of a wide split (same slots as the single-CTA kernel) and the
 // new bond dimension.
-__global__ void k_wide_commit(double* stats, int* bond, int b, const WideEigStatus* st, double flops,
+__global__ void k_wide_commit(double* stats, int* bond, int b, int k, double total, double kept, double flops,
                               double eig_flops) {
-  const double total = st->total, kept = st->kept;
   const double frac = total > 0.0 ? (total - kept) / total : 0.0;
   stats[ST_LOG_FID] += log1p(-(frac < 1.0 ? frac : 0.0));
   if (frac > stats[ST_MAX_DISC]) stats[ST_MAX_DISC] = frac;
@@ -158,7 +155,17 @@ __global__ void k_wide_commit(double* stats, int* bond, int b, const WideEigStat
   stats[ST_N_OPS] += 1.0;
   stats[ST_FLOPS] += flops;
   stats[ST_EIG_FLOPS] += eig_flops;
-  bond[b] = st->k;
+  bond[b] = k;
+}
+// Z = X (strided view) copied into a compact m x nn buffer.
+template <typename T>
+__global__ void k_copy_view(CMat<T> X, cx<T>* Z) {
+  const int nn = X.cols;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < (int64_t)X.rows * nn;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(t / nn), c = (int)(t - (int64_t)i * nn);
+    Z[t] = X.p[(int64_t)i * X.rs + (int64_t)c * X.cs];
+  }
 }
 __global__ void k_set_bond(double* stats, int* bond, int b, int v, double flops) {
   if (b >= 0) bond[b] = v;
@@ -253,14 +260,17 @@ struct WideBufs {
   void* Y = nullptr;
   void* S = nullptr;
   void* R = nullptr;
+  void* gram2 = nullptr;  // Gram of the deflated tail
+  void* Z = nullptr;      // deflated X
   void* scal = nullptr;  // iso, oth, inv (3 m of T)
   double* lam = nullptr;
   void* eig_work = nullptr;
+  void* eig_work2 = nullptr;
   void* qr_work = nullptr;
-  WideEigStatus* d_status = nullptr;
+  int* d_status = nullptr;     // grid-barrier status of the cooperative launches
   double* d_scalar = nullptr;  // 2 doubles
   int* d_err = nullptr;
-  char* h_pinned = nullptr;  // status + scalars
+  char* h_pinned = nullptr;    // [0, 256): scalars; then 2 x kWideM doubles of eigenvalues
   GemmWs gemm;
 };
 
@@ -269,8 +279,8 @@ struct WideAll {
 };
 
 static void wide_bufs_free(WideBufs& B) {
-  void* ptrs[] = {B.theta, B.tbuf, B.gram, B.W, B.W2, B.W3, B.Y, B.S, B.R, B.scal, B.lam, B.eig_work, B.qr_work,
-                  B.d_status, B.d_scalar, B.d_err};
+  void* ptrs[] = {B.theta, B.tbuf, B.gram, B.W, B.W2, B.W3, B.Y, B.S, B.R, B.gram2, B.Z, B.scal, B.lam,
+                  B.eig_work, B.eig_work2, B.qr_work, B.d_status, B.d_scalar, B.d_err};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   if (B.h_pinned) cudaFreeHost(B.h_pinned);
@@ -297,17 +307,18 @@ static int wide_bufs(mps_ctx* c, int prec, int chi, WideBufs** out) {
   wide_bufs_free(B);
   const size_t eb = prec == MPS_PREC_FP64 ? 16 : 8;
   const size_t E = (size_t)m * m;
-  void** big[] = {&B.theta, &B.tbuf, &B.gram, &B.W, &B.W2, &B.W3, &B.Y, &B.S, &B.R};
+  void** big[] = {&B.theta, &B.tbuf, &B.gram, &B.W, &B.W2, &B.W3, &B.Y, &B.S, &B.R, &B.gram2, &B.Z};
   bool ok = true;
   for (void** q : big) ok = ok && cudaMalloc(q, E * eb) == cudaSuccess;
   ok = ok && cudaMalloc(&B.scal, 3 * (size_t)m * eb) == cudaSuccess;
   ok = ok && cudaMalloc(&B.lam, (size_t)m * sizeof(double)) == cudaSuccess;
   ok = ok && cudaMalloc(&B.eig_work, wide_eig_work_bytes(prec, m)) == cudaSuccess;
+  ok = ok && cudaMalloc(&B.eig_work2, wide_eig_work_bytes(prec, m)) == cudaSuccess;
   ok = ok && cudaMalloc(&B.qr_work, wide_qr_work_bytes(prec, m, m)) == cudaSuccess;
-  ok = ok && cudaMalloc(&B.d_status, sizeof(WideEigStatus)) == cudaSuccess;
+  ok = ok && cudaMalloc(&B.d_status, 16) == cudaSuccess;
   ok = ok && cudaMalloc(&B.d_scalar, 4 * sizeof(double)) == cudaSuccess;
   ok = ok && cudaMalloc(&B.d_err, sizeof(int)) == cudaSuccess;
-  ok = ok && cudaMallocHost(&B.h_pinned, 256) == cudaSuccess;
+  ok = ok && cudaMallocHost(&B.h_pinned, 256 + 2 * sizeof(double) * (size_t)kWideM) == cudaSuccess;
   // tensor-core operands: A side up to m x 2m, B side up to 2m x 2m (padded)
   if (ok && prec == MPS_PREC_FP32) {
     const size_t pad = (size_t)(m + 128) * (2 * m + 128);
@@ -337,20 +348,22 @@ static int blocks_for(int64_t n) { return (int)std::min<int64_t>((n + 255) / 256
 
 // ------------------------------------------------------------ two-site update
 template <typename T>
-static int orthonormalize_w(WideBufs& B, const CMat<T>& X, int m, int nn, int k, cx<T>* Wc, bool subspace,
+static int orthonormalize_w(WideBufs& B, const CMat<T>& X, int m, int nn, int kk, int ld, cx<T>* Wc, bool subspace,
                             cudaStream_t st, cx<T>** result, double* ortho_flops) {
-  // Wc: m x k (ld k).  Returns the orthonormal columns in *result (ld k).
+  // Wc: m x kk (row stride ld).  Returns the orthonormal columns in *result
+  // (m x kk, row stride ld); columns kk..ld-1 of the result are unspecified.
   cx<T>* cur = Wc;
   cx<T>* nxt = reinterpret_cast<cx<T>*>(cur == B.W3 ? B.W2 : B.W3);
   cx<T>* S = reinterpret_cast<cx<T>*>(B.S);
   double* hs = reinterpret_cast<double*>(B.h_pinned + 128);
   const double ns_stop = sizeof(T) == 4 ? 1e-4 : 1e-8;
   bool qr_taken = false;
+  auto view = [&](cx<T>* p) { return cmat<T>(p, m, kk, ld, 1); };
+  auto oview = [&](cx<T>* p) { return cout_<T>(p, m, kk, ld, 1); };
   for (int it = 0; it < 5; ++it) {
-    WCK(cgemm(adj(cmat<T>(cur, m, k, k, 1)), cmat<T>(cur, m, k, k, 1), cout_<T>(S, k, k, k, 1), T(1), T(0), B.gemm,
-              st));
-    *ortho_flops += 8.0 * k * k * m;
-    k_defect<T><<<1, 256, 0, st>>>(S, k, B.d_scalar);
+    WCK(cgemm(adj(view(cur)), view(cur), cout_<T>(S, kk, kk, kk, 1), T(1), T(0), B.gemm, st));
+    *ortho_flops += 8.0 * kk * kk * m;
+    k_defect<T><<<1, 256, 0, st>>>(S, kk, B.d_scalar);
     WCK(cudaMemcpyAsync(hs, B.d_scalar, sizeof(double), cudaMemcpyDeviceToHost, st));
     WCK(cudaStreamSynchronize(st));
     const double fro = hs[0];
@@ -359,10 +372,9 @@ static int orthonormalize_w(WideBufs& B, const CMat<T>& X, int m, int nn, int k,
       qr_taken = true;
       break;
     }
-    WCK(cudaMemcpyAsync(nxt, cur, (size_t)m * k * sizeof(cx<T>), cudaMemcpyDeviceToDevice, st));
-    WCK(cgemm(cmat<T>(cur, m, k, k, 1), cmat<T>(S, k, k, k, 1), cout_<T>(nxt, m, k, k, 1), T(-0.5), T(1.5), B.gemm,
-              st));
-    *ortho_flops += 8.0 * k * k * m;
+    WCK(cudaMemcpyAsync(nxt, cur, (size_t)m * ld * sizeof(cx<T>), cudaMemcpyDeviceToDevice, st));
+    WCK(cgemm(view(cur), cmat<T>(S, kk, kk, kk, 1), oview(nxt), T(-0.5), T(1.5), B.gemm, st));
+    *ortho_flops += 8.0 * kk * kk * m;
     std::swap(cur, nxt);
     if (fro < ns_stop) break;
   }
@@ -371,24 +383,65 @@ static int orthonormalize_w(WideBufs& B, const CMat<T>& X, int m, int nn, int k,
     // from rounding noise) one subspace step with X and a second QR
     const int grid = coop_grid(sizeof(T) == 8 ? 0 : 1, 1);
     for (int pass = 0; pass < 2; ++pass) {
-      WCK(launch_wide_qr_t<T>(cmat<T>(cur, m, k, k, 1), cout_<T>(nxt, m, k, k, 1), 0, B.R, B.qr_work, B.d_err, grid,
-                              st));
+      WCK(launch_wide_qr_t<T>(view(cur), oview(nxt), 0, B.R, B.qr_work, B.d_err, grid, st));
       std::swap(cur, nxt);
-      if (pass == 1 || k >= m || !subspace) break;
+      if (pass == 1 || kk >= m || !subspace) break;
       cx<T>* Y = reinterpret_cast<cx<T>*>(B.Y);
-      WCK(cgemm(adj(X), cmat<T>(cur, m, k, k, 1), cout_<T>(Y, nn, k, k, 1), T(1), T(0), B.gemm, st));
-      WCK(cgemm(X, cmat<T>(Y, nn, k, k, 1), cout_<T>(nxt, m, k, k, 1), T(1), T(0), B.gemm, st));
+      WCK(cgemm(adj(X), view(cur), cout_<T>(Y, nn, kk, kk, 1), T(1), T(0), B.gemm, st));
+      WCK(cgemm(X, cmat<T>(Y, nn, kk, kk, 1), oview(nxt), T(1), T(0), B.gemm, st));
       T* inv = reinterpret_cast<T*>(B.scal) + 2 * B.m;
-      k_colnorm<T><<<(k + 255) / 256, 256, 0, st>>>(nxt, m, k, cur, k, inv);
-      k_colscale<T><<<blocks_for((int64_t)m * k), 256, 0, st>>>(nxt, m, k, inv);
+      k_colnorm<T><<<(kk + 255) / 256, 256, 0, st>>>(nxt, m, kk, ld, cur, ld, inv);
+      k_colscale<T><<<blocks_for((int64_t)m * kk), 256, 0, st>>>(nxt, m, kk, ld, inv);
       std::swap(cur, nxt);
-      *ortho_flops += 16.0 * m * nn * k;
+      *ortho_flops += 16.0 * m * nn * kk;
     }
     int herr = 0;
     WCK(cudaMemcpy(&herr, B.d_err, sizeof(int), cudaMemcpyDeviceToHost));
     if (herr) return fail(MPS_ERR_TIMEOUT, "cooperative QR gave up at a grid barrier");
   }
   *result = cur;
+  return MPS_OK;
+}
+
+// Eigenvalues (descending) of the m x m Gram G into h_lam (host, pinned);
+// the reflectors stay in G and the work buffer for eig_vectors.
+template <typename T>
+static int eig_values(WideBufs& B, void* G, void* work, int m, double* h_lam, cudaStream_t st) {
+  const int prec = sizeof(T) == 8 ? 0 : 1;
+  WideEigArgs ea;
+  std::memset(&ea, 0, sizeof(ea));
+  ea.G = G;
+  ea.lam = B.lam;
+  ea.m = m;
+  ea.phase = 0;
+  ea.work = work;
+  ea.status_err = B.d_status;
+  WCK(launch_wide_eig(prec, ea, coop_grid(prec, 0), st));
+  int* herr = reinterpret_cast<int*>(B.h_pinned + 64);
+  WCK(cudaMemcpyAsync(h_lam, B.lam, sizeof(double) * m, cudaMemcpyDeviceToHost, st));
+  WCK(cudaMemcpyAsync(herr, B.d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
+  WCK(cudaStreamSynchronize(st));
+  if (*herr) return fail(MPS_ERR_TIMEOUT, "cooperative eigensolver gave up at a grid barrier");
+  for (int i = 0; i < m; ++i)
+    if (!std::isfinite(h_lam[i])) return fail(MPS_ERR_NUMERIC, "non-finite value in a wide split");
+  return MPS_OK;
+}
+
+// Eigenvectors of ranks 0..kv-1 into W (m x kv, row stride ld).
+template <typename T>
+static int eig_vectors(WideBufs& B, void* G, void* work, int m, int kv, void* W, int ld, cudaStream_t st) {
+  const int prec = sizeof(T) == 8 ? 0 : 1;
+  WideEigArgs ea;
+  std::memset(&ea, 0, sizeof(ea));
+  ea.G = G;
+  ea.W = W;
+  ea.m = m;
+  ea.phase = 1;
+  ea.kv = kv;
+  ea.ld = ld;
+  ea.work = work;
+  ea.status_err = B.d_status;
+  WCK(launch_wide_eig(prec, ea, coop_grid(prec, 0), st));
   return MPS_OK;
 }
 
@@ -419,54 +472,124 @@ static int wide_gate2(mps_prog* p, WideBufs& B, cudaStream_t st, const DevOp& op
   cx<T>* G = reinterpret_cast<cx<T>*>(B.gram);
   WCK(cgemm(X, adj(X), cout_<T>(G, m, m, m, 1), T(1), T(0), B.gemm, st));
   const int kcap = std::min(p->chi_cap, mm);
-  WideEigArgs ea;
-  ea.G = G;
-  ea.W = B.W;
-  ea.lam = B.lam;
-  ea.m = m;
-  ea.mm = mm;
-  ea.kcap = kcap;
-  ea.mode = p->mode;
-  ea.cutoff = p->cutoff;
-  ea.work = B.eig_work;
-  ea.status = B.d_status;
-  const int prec = sizeof(T) == 8 ? 0 : 1;
-  WCK(launch_wide_eig(prec, ea, coop_grid(prec, 0), st));
-  WideEigStatus* hst = reinterpret_cast<WideEigStatus*>(B.h_pinned);
-  int* hbar = reinterpret_cast<int*>(B.h_pinned + 64);
-  WCK(cudaMemcpyAsync(hst, B.d_status, sizeof(WideEigStatus), cudaMemcpyDeviceToHost, st));
-  WCK(cudaMemcpyAsync(hbar, B.eig_work, 16, cudaMemcpyDeviceToHost, st));
-  WCK(cudaStreamSynchronize(st));
-  if (hbar[2]) return fail(MPS_ERR_TIMEOUT, "cooperative eigensolver gave up at a grid barrier");
-  if (hst->err & ERR_NAN) return fail(MPS_ERR_NUMERIC, "non-finite value in a wide split");
-  const int k = hst->k;
-  if (k < 1 || k > kcap) return fail(MPS_ERR_NUMERIC, "wide split returned an invalid bond dimension");
-  // W (m x k, ld kcap) -> compact (ld k) in W2, [subspace step], orthonormalise
-  cx<T>* Wk = reinterpret_cast<cx<T>*>(B.W2);
-  WCK(cudaMemcpy2DAsync(Wk, (size_t)k * sizeof(cx<T>), B.W, (size_t)kcap * sizeof(cx<T>), (size_t)k * sizeof(cx<T>),
-                        m, cudaMemcpyDeviceToDevice, st));
-  double extra = 0.0;
+  double* hl = reinterpret_cast<double*>(B.h_pinned + 256);
+  double* hl2 = hl + kWideM;
+  int rc = eig_values<T>(B, G, B.eig_work, m, hl, st);
+  if (rc) return rc;
   const bool fp32 = sizeof(T) == 4;
-  if (fp32 && k < m) {
+  double extra = 0.0, eig_flops = (32.0 / 3.0) * m * m * m;
+  std::vector<double> lk(hl, hl + mm);
+  int k = keep_rule(lk.data(), mm, p->mode, p->cutoff, kcap);
+  cx<T>* Wk = reinterpret_cast<cx<T>*>(B.W2);  // kept vectors, m x k (row stride k)
+  // FP32 refinement: an FP32 Gram resolves eigenvalues only down to ~eps *
+  // lambda_max.  When the cut falls below kRefine * lambda_max, the tail is
+  // re-solved in the complement of the head (the eigenvectors above that
+  // ratio): Z = X - W_h (W_h^H X) has the size of the tail and its Gram
+  // resolves it to ~eps * |Z|^2 (ITensor's recursive refinement of small
+  // singular values, SVDRefImpl, tensor/algs.cc:510-579, one level deep).
+  constexpr double kRefine = 1e-4;
+  int s_head = 0;
+  while (s_head < mm && hl[s_head] >= kRefine * hl[0]) ++s_head;
+  const bool refine = fp32 && hl[0] > 0.0 && k > s_head && s_head < m;
+  if (refine) {
+    cx<T>* Wh = reinterpret_cast<cx<T>*>(B.W);
+    rc = eig_vectors<T>(B, G, B.eig_work, m, s_head, Wh, s_head, st);
+    if (rc) return rc;
+    cx<T>* Who = nullptr;
+    rc = orthonormalize_w<T>(B, X, m, nn, s_head, s_head, Wh == reinterpret_cast<cx<T>*>(B.W3) ? Wh : Wh, false, st,
+                             &Who, &extra);
+    if (rc) return rc;
+    // keep W_h in B.W (the buffers W2/W3 serve the orthonormalisation)
+    if (Who != Wh)
+      WCK(cudaMemcpyAsync(Wh, Who, (size_t)m * s_head * sizeof(cx<T>), cudaMemcpyDeviceToDevice, st));
+    cx<T>* Y = reinterpret_cast<cx<T>*>(B.Y);
+    cx<T>* Z = reinterpret_cast<cx<T>*>(B.Z);
+    WCK(cgemm(adj(cmat<T>(Wh, m, s_head, s_head, 1)), X, cout_<T>(Y, s_head, nn, nn, 1), T(1), T(0), B.gemm, st));
+    k_copy_view<T><<<blocks_for((int64_t)m * nn), 256, 0, st>>>(X, Z);
+    WCK(cgemm(cmat<T>(Wh, m, s_head, s_head, 1), cmat<T>(Y, s_head, nn, nn, 1), cout_<T>(Z, m, nn, nn, 1), T(-1),
+              T(1), B.gemm, st));
+    const CMat<T> Zv = cmat<T>(Z, m, nn, nn, 1);
+    cx<T>* G2 = reinterpret_cast<cx<T>*>(B.gram2);
+    WCK(cgemm(Zv, adj(Zv), cout_<T>(G2, m, m, m, 1), T(1), T(0), B.gemm, st));
+    rc = eig_values<T>(B, G2, B.eig_work2, m, hl2, st);
+    if (rc) return rc;
+    extra += 16.0 * m * s_head * nn + 8.0 * m * m * nn;
+    eig_flops *= 2.0;
+    // combined spectrum: the head from G, the tail from the deflated Gram;
+    // tail values below ~eps^2 * lambda_max are its rounding noise
+    const double floor_t = 64.0 * 1.4210854715202004e-14 * hl[0];
+    for (int i = s_head; i < mm; ++i) {
+      const double v = hl2[i - s_head];
+      lk[i] = v > floor_t ? v : 0.0;
+    }
+    k = keep_rule(lk.data(), mm, p->mode, p->cutoff, kcap);
+    // kept vectors: head columns, then the tail's leading eigenvectors made
+    // orthogonal to the head (Gram-Schmidt, as Z's rounding leaves small
+    // components along W_h)
+    const int ks = std::min(k, s_head), kt = k - ks;
+    WCK(cudaMemcpy2DAsync(Wk, (size_t)k * sizeof(cx<T>), Wh, (size_t)s_head * sizeof(cx<T>),
+                          (size_t)ks * sizeof(cx<T>), m, cudaMemcpyDeviceToDevice, st));
+    if (kt > 0) {
+      rc = eig_vectors<T>(B, G2, B.eig_work2, m, kt, Wk + ks, k, st);
+      if (rc) return rc;
+      cx<T>* P = reinterpret_cast<cx<T>*>(B.S);
+      WCK(cgemm(adj(cmat<T>(Wh, m, s_head, s_head, 1)), cmat<T>(Wk + ks, m, kt, k, 1),
+                cout_<T>(P, s_head, kt, kt, 1), T(1), T(0), B.gemm, st));
+      WCK(cgemm(cmat<T>(Wh, m, s_head, s_head, 1), cmat<T>(P, s_head, kt, kt, 1), cout_<T>(Wk + ks, m, kt, k, 1),
+                T(-1), T(1), B.gemm, st));
+      extra += 16.0 * m * s_head * kt;
+    }
+  } else {
+    rc = eig_vectors<T>(B, G, B.eig_work, m, k, Wk, k, st);
+    if (rc) return rc;
+  }
+  eig_flops += 8.0 * m * m * k;
+  double total = 0.0, kept = 0.0;
+  int kpos = 0;
+  for (int i = 0; i < mm; ++i) {
+    const double v = lk[i] > 0.0 ? lk[i] : 0.0;
+    total += v;
+    if (i < k) {
+      kept += v;
+      kpos += v > 0.0;
+    }
+  }
+  if (k < 1 || k > kcap) return fail(MPS_ERR_NUMERIC, "wide split returned an invalid bond dimension");
+  // columns with zero weight are scaled by 0 (exatn) or never kept (itensor),
+  // so only the first kk need to be orthonormal
+  const int kk = std::max(1, std::min(k, kpos));
+  if (fp32 && kk < m) {
+    // one subspace step W <- X (X^H W) with X itself: the Gram's rounding
+    // tilts a kept eigenvector by ~eps * lambda_max / lambda, the product's
+    // only by ~eps * sigma_max / sigma
     cx<T>* Y = reinterpret_cast<cx<T>*>(B.Y);
     cx<T>* W3 = reinterpret_cast<cx<T>*>(B.W3);
-    WCK(cgemm(adj(X), cmat<T>(Wk, m, k, k, 1), cout_<T>(Y, nn, k, k, 1), T(1), T(0), B.gemm, st));
-    WCK(cgemm(X, cmat<T>(Y, nn, k, k, 1), cout_<T>(W3, m, k, k, 1), T(1), T(0), B.gemm, st));
+    WCK(cgemm(adj(X), cmat<T>(Wk, m, kk, k, 1), cout_<T>(Y, nn, kk, kk, 1), T(1), T(0), B.gemm, st));
+    WCK(cgemm(X, cmat<T>(Y, nn, kk, kk, 1), cout_<T>(W3, m, kk, k, 1), T(1), T(0), B.gemm, st));
     T* inv = reinterpret_cast<T*>(B.scal) + 2 * B.m;
-    k_colnorm<T><<<(k + 255) / 256, 256, 0, st>>>(W3, m, k, Wk, k, inv);
-    k_colscale<T><<<blocks_for((int64_t)m * k), 256, 0, st>>>(W3, m, k, inv);
-    extra += 16.0 * m * nn * k;
+    k_colnorm<T><<<(kk + 255) / 256, 256, 0, st>>>(W3, m, kk, k, Wk, k, inv);
+    k_colscale<T><<<blocks_for((int64_t)m * kk), 256, 0, st>>>(W3, m, kk, k, inv);
+    if (kk < k)  // zero-weight columns: carried over unchanged (scaled by 0 below)
+      WCK(cudaMemcpy2DAsync(W3 + kk, (size_t)k * sizeof(cx<T>), Wk + kk, (size_t)k * sizeof(cx<T>),
+                            (size_t)(k - kk) * sizeof(cx<T>), m, cudaMemcpyDeviceToDevice, st));
+    extra += 16.0 * m * nn * kk;
     Wk = W3;
   }
   cx<T>* Wf = nullptr;
-  int rc = orthonormalize_w<T>(B, X, m, nn, k, Wk, true, st, &Wf, &extra);
+  rc = orthonormalize_w<T>(B, X, m, nn, kk, k, Wk, true, st, &Wf, &extra);
   if (rc) return rc;
+  if (Wf != Wk && kk < k)
+    WCK(cudaMemcpy2DAsync(Wf + kk, (size_t)k * sizeof(cx<T>), Wk + kk, (size_t)k * sizeof(cx<T>),
+                          (size_t)(k - kk) * sizeof(cx<T>), m, cudaMemcpyDeviceToDevice, st));
+  // scales from the kept eigenvalues
+  double* hk = reinterpret_cast<double*>(B.h_pinned + 256) + kWideM;
+  for (int i = 0; i < k; ++i) hk[i] = lk[i] > 0.0 ? lk[i] : 0.0;
+  WCK(cudaMemcpyAsync(B.lam, hk, sizeof(double) * k, cudaMemcpyHostToDevice, st));
+  const double rn = ((p->flags & MPS_FLAG_RENORM) && kept > 0.0) ? std::sqrt(total / kept) : 1.0;
   T* iso = reinterpret_cast<T*>(B.scal);
   T* oth = iso + B.m;
-  k_split_scales<T><<<(k + 255) / 256, 256, 0, st>>>(B.lam, B.d_status, op.orient == ORIENT_SQRT ? 1 : 0,
-                                                     (p->flags & MPS_FLAG_RENORM) ? 1 : 0, iso, oth);
-  cx<T>* Wo = reinterpret_cast<cx<T>*>(Wf == B.W2 ? B.W3 : B.W2);
-  if (Wo == Wf) Wo = reinterpret_cast<cx<T>*>(B.Y);
+  k_split_scales<T><<<(k + 255) / 256, 256, 0, st>>>(B.lam, k, op.orient == ORIENT_SQRT ? 1 : 0, rn, iso, oth);
+  cx<T>* Wo = reinterpret_cast<cx<T>*>(Wf == reinterpret_cast<cx<T>*>(B.W2) ? B.W3 : B.W2);
   if (!tr) {
     k_write_iso<T><<<blocks_for((int64_t)m * k), 256, 0, st>>>(Wf, m, k, iso, oth, 0, A, Wo);
     WCK(cgemm(adj(cmat<T>(Wo, m, k, k, 1)), X, cout_<T>(Bs, k, Cc, Cc, 1), T(1), T(0), B.gemm, st));
@@ -476,9 +599,13 @@ static int wide_gate2(mps_prog* p, WideBufs& B, cudaStream_t st, const DevOp& op
               B.gemm, st));
   }
   const double flops = 32.0 * dl * dm * dr + 128.0 * dl * dr + 8.0 * m * m * nn + 8.0 * k * nn * m + extra;
-  const double eig_flops = (32.0 / 3.0) * m * m * m + 8.0 * m * m * k;
-  k_wide_commit<<<1, 1, 0, st>>>(p->d_stats, p->d_bond, lo + 1, B.d_status, flops, eig_flops);
+  k_wide_commit<<<1, 1, 0, st>>>(p->d_stats, p->d_bond, lo + 1, k, total, kept, flops, eig_flops);
   WCK(cudaGetLastError());
+  // the host buffer hk must outlive the copy above
+  WCK(cudaStreamSynchronize(st));
+  int herr = 0;
+  WCK(cudaMemcpy(&herr, B.d_status, sizeof(int), cudaMemcpyDeviceToHost));
+  if (herr) return fail(MPS_ERR_TIMEOUT, "cooperative eigensolver gave up at a grid barrier");
   p->hbond[lo + 1] = k;
   return MPS_OK;
 }

@@ -91,27 +91,25 @@ cudaError_t cgemm_simt(const CMat<float>& A, const CMat<float>& B, const CMatOut
                        float beta, cudaStream_t st);
 
 // ------------------------------------------------------------ cooperative
-// Result of one wide eigen-decomposition (device struct, read back by the host).
-struct WideEigStatus {
-  int32_t k;        // kept dimension
-  int32_t err;      // ERR_* bits, plus kCoopTimeout
-  double total;     // sum of the (clamped) eigenvalues
-  double kept;      // sum of the kept ones
-  double lam_max;
-};
 constexpr int32_t kCoopTimeout = 1 << 8;
 
+// Eigen-decomposition of the m x m Hermitian Gram matrix G (row-major, ld m)
+// in two cooperative launches.  phase 0: tridiagonalisation (the reflectors
+// overwrite G), every eigenvalue, descending order -> lam[0..m).  phase 1:
+// eigenvectors of ranks 0..kv-1 -> columns of W (row stride ld).  The work
+// buffer carries the state from phase 0 to phase 1; status_err receives
+// kCoopTimeout when a grid barrier gave up.
 struct WideEigArgs {
-  void* G;          // m x m Hermitian (row-major, ld m), destroyed (holds the reflectors)
-  void* W;          // out: m x kcap kept eigenvectors (row-major, ld kcap)
-  double* lam;      // out: m eigenvalues, descending
+  void* G;
+  void* W;
+  double* lam;
   int m;
-  int mm;           // singular values of the split (min side of theta); the keep rule reads lam[0..mm)
-  int kcap;         // largest k allowed (chi cap); the keep rule picks k <= kcap
-  int mode;         // TRUNC_EXATN / TRUNC_ITENSOR
-  double cutoff;
+  int phase;
+  int kv;
+  int ld;
+  int grid0;        // grid of the launches (work-buffer layout); set by launch_wide_eig
   void* work;       // cooperative scratch (wide_eig_work_bytes)
-  WideEigStatus* status;
+  int* status_err;
 };
 size_t wide_eig_work_bytes(int prec, int m);
 cudaError_t launch_wide_eig(int prec, const WideEigArgs& a, int grid, cudaStream_t st);
