@@ -82,7 +82,7 @@ int mps_ctx_info(mps_ctx* ctx, int* num_sms, size_t* bytes_resident);
  * |0...0> with every bond of dimension 1.  chi_max <= 0 means "no cap"
  * (clamped to MPS_CHI_LIMIT); caps up to MPS_WIDE_CHI_LIMIT are accepted,
  * those above MPS_CHI_LIMIT run gate by gate on the wide path (not with
- * MPS_FLAG_PER_GATE, captured graphs or the serve loop).  cutoff < 0 selects
+ * MPS_FLAG_PER_GATE or in captured graphs).  cutoff < 0 selects
  * the visitor's default (DBL_MIN for exatn, 1e-6 for itensor). */
 int mps_program_begin(mps_ctx* ctx, int n_qubits, int chi_max, double cutoff,
                       int trunc_mode, int precision, int flags, mps_prog** out);
@@ -182,7 +182,9 @@ int mps_graph_destroy(mps_graph* g);
 /* Continuous-batching request loop (serving).  Requests are programs that
  * have recorded gates and optionally an observable and a shot count; the
  * loop admits them by projected HBM footprint, runs them in overlapping
- * persistent launches and completes them out of order. */
+ * persistent launches and completes them out of order.  Requests whose bond
+ * cap exceeds MPS_CHI_LIMIT run one at a time on a separate wide lane that
+ * overlaps the batches. */
 int mps_serve_start(mps_ctx* ctx, int max_inflight);
 int mps_serve_submit(mps_ctx* ctx, mps_prog* p, int shots, uint64_t seed, uint64_t* ticket);
 /* Polls a ticket: returns MPS_OK when done (result written), MPS_ERR_TIMEOUT

@@ -141,3 +141,47 @@ def test_wide_rejections(ctx):
     with pytest.raises(M.MpsError) as e:
         M.Program(ctx, 20, 128, -1.0, M.TRUNC_EXATN, M.PREC_FP64, M.FLAG_PER_GATE)
     assert e.value.code == M.ERR_UNSUPPORTED
+
+
+def test_wide_serve_same_alone_and_in_mix(ctx):
+    """Requests with bond caps 16, 64, 128 and 256 in one Poisson-free burst:
+    each wide request's energy and shots equal its result when served alone,
+    and the narrow ones still complete beside it."""
+    rng = np.random.default_rng(12)
+    specs = []
+    for i in range(12):
+        n = int(rng.integers(10, 17))
+        chi = [16, 64, 128, 256][i % 4]
+        circ = circuits.brickwall(n, int(rng.integers(4, 9)), seed=100 + i)
+        paulis, coeffs = circuits.random_paulis(n, 4, rng)
+        specs.append((n, chi, circ, paulis, coeffs))
+
+    def make(spec):
+        n, chi, circ, paulis, coeffs = spec
+        p = M.Program(ctx, n, chi, 1e-12, M.TRUNC_ITENSOR, M.PREC_FP32)
+        p.run(circ)
+        p.set_observable(paulis, coeffs)
+        return p
+
+    wide = [i for i, sp in enumerate(specs) if sp[1] > M.CHI_LIMIT]
+    alone = {}
+    ctx.serve_start(64)
+    try:
+        for i in wide:
+            p = make(specs[i])
+            t = ctx.serve_submit(p, 128, 9)
+            e, bits, _ = ctx.serve_poll(t, p, 128)
+            alone[i] = (e, bits.copy())
+            p.close()
+        progs = [make(sp) for sp in specs]
+        tickets = [ctx.serve_submit(p, 128, 9) for p in progs]
+        for i, (t, p) in enumerate(zip(tickets, progs)):
+            e, bits, lat = ctx.serve_poll(t, p, 128)
+            assert lat >= 0.0 and np.isfinite(e)
+            if i in alone:
+                assert abs(e - alone[i][0]) < 1e-9
+                assert np.array_equal(bits, alone[i][1])
+        for p in progs:
+            p.close()
+    finally:
+        ctx.serve_stop()

@@ -90,6 +90,13 @@ struct ServeBatch {
 
 struct ServeState {
   std::thread worker;
+  // wide requests (bond cap above the single-CTA limit) run one at a time on
+  // their own worker, lane and workspace, overlapping the batched lanes
+  std::thread wide_worker;
+  std::deque<ServeReq*> wide_queue;
+  std::condition_variable cv_wide;
+  Lane wide_lane;
+  void* wide_ws = nullptr;
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
   std::deque<ServeReq*> queue;
@@ -160,9 +167,14 @@ void observable_tasks(::mps_prog* p, std::vector<ExpTask>& tasks);
 double observable_value(const ::mps_prog* p, const double* r);
 // wide path (wide.cu): bond caps above the single-CTA limit
 bool prog_is_wide(const ::mps_prog* p);
-int wide_run(mps_ctx* c, Lane& L, ::mps_prog* p);
-int wide_expect(::mps_prog* p, const uint8_t* codes, int n_terms, double* out);
-int wide_sample(::mps_prog* p, int shots, uint64_t seed, uint8_t* h_all_bits);
+// ws: the wide workspace to use (nullptr: the context's); L: the lane whose
+// stream runs the work (nullptr: the context's lane 0)
+int wide_run(mps_ctx* c, Lane& L, ::mps_prog* p, void** ws = nullptr);
+int wide_expect(::mps_prog* p, const uint8_t* codes, int n_terms, double* out, Lane* L = nullptr,
+                void** ws = nullptr);
+int wide_sample(::mps_prog* p, int shots, uint64_t seed, uint8_t* h_all_bits, Lane* L = nullptr,
+                void** ws = nullptr);
+void wide_ws_free(void** ws);
 int wide_amp_one(::mps_prog* p, const int* bits, double* out);
 int wide_gemm_counts(mps_ctx* c, int* tc, int* simt);
 int wide_diag_cgemm(mps_ctx* c, int M, int N, int K, const double* a, const double* b, double* out_tc,

@@ -666,6 +666,7 @@ template <typename T>
 __global__ void __launch_bounds__(kCoopThreads, 1) k_wide_qr(QrArgsT<T> a) {
   __shared__ cx<T> tile[32][33];
   __shared__ cx<T> s_red[kCoopWarps];
+  __shared__ T s_sum[kCoopWarps];
   const int mr = a.M.rows, nc = a.M.cols, k = mr < nc ? mr : nc;
   const int G = gridDim.x, cta = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   QrWork<T> wk = qr_work<T>(a.work, mr, nc);
@@ -685,13 +686,13 @@ __global__ void __launch_bounds__(kCoopThreads, 1) k_wide_qr(QrArgsT<T> a) {
   const T tiny = T(CoopPrec<T>::tiny);
   // 1. reflectors; column c is owned by CTA c % G, one warp per owned column
   for (int j = 0; j < k; ++j) {
-    if (j % G == cta && warp == 0) {
+    if (j % G == cta) {
+      // the whole owner CTA forms reflector j (block-wide norm)
       cx<T>* x = wk.MT + (int64_t)j * mr;  // own column (written by other CTAs in step 0: read via L2)
-      T s = T(0);
-      for (int i = j + 1 + lane; i < mr; i += 32) s += abs2(ldcg(x + i));
-      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      T s_part = T(0);
+      for (int i = j + 1 + tid; i < mr; i += kCoopThreads) s_part += abs2(ldcg(x + i));
+      const T s = coop_sum<T>(s_part, s_sum);
       const cx<T> alpha = ldcg(x + j);
-      __syncwarp();
       const T ar = alpha.re, ai = alpha.im;
       const T nrm2 = ar * ar + ai * ai + s;
       const bool refl = !(s == T(0) && ai == T(0)) && nrm2 > tiny;
@@ -701,14 +702,14 @@ __global__ void __launch_bounds__(kCoopThreads, 1) k_wide_qr(QrArgsT<T> a) {
         const T dr = ar - beta, di = ai, den = dr * dr + di * di;
         const T ir = dr / den, ii = -di / den;
         tau = mk<T>((beta - ar) / beta, -ai / beta);
-        for (int i = j + 1 + lane; i < mr; i += 32) {
+        for (int i = j + 1 + tid; i < mr; i += kCoopThreads) {
           const cx<T> v = ldcg(x + i);
           stcg(x + i, mk<T>(v.re * ir - v.im * ii, v.re * ii + v.im * ir));
         }
-        __syncwarp();
-        if (lane == 0) stcg(x + j, mk<T>(beta, T(0)));
+        __syncthreads();  // every thread has read alpha
+        if (tid == 0) stcg(x + j, mk<T>(beta, T(0)));
       }
-      if (lane == 0) stcg(wk.tau + j, tau);
+      if (tid == 0) stcg(wk.tau + j, tau);
     }
     if (!grid_sync(wk.bar)) return;
     const cx<T> tj = ldcg(wk.tau + j);

@@ -170,6 +170,55 @@ static void serve_loop(mps_ctx* c) {
   }
 }
 
+// Wide requests: one at a time on the wide lane (host-driven splits),
+// admitted under the same HBM footprint budget as the batches.
+static void serve_wide_loop(mps_ctx* c) {
+  cudaSetDevice(c->device);
+  ServeState* S = c->serve;
+  for (;;) {
+    ServeReq* r = nullptr;
+    {
+      std::unique_lock<std::mutex> lk(S->mu);
+      S->cv_wide.wait_for(lk, std::chrono::milliseconds(5), [&] { return S->stop || !S->wide_queue.empty(); });
+      if (S->wide_queue.empty()) {
+        if (S->stop) break;
+        continue;
+      }
+      ServeReq* head = S->wide_queue.front();
+      if (S->inflight_reqs > 0 && S->inflight_bytes + head->prog->bytes > c->budget) continue;
+      r = head;
+      S->wide_queue.pop_front();
+      S->inflight_bytes += r->prog->bytes;
+      S->inflight_reqs += 1;
+    }
+    mps_prog* p = r->prog;
+    int rc = wide_run(c, S->wide_lane, p, &S->wide_ws);
+    double energy = 0.0;
+    std::vector<uint8_t> all;
+    if (!rc && p->d_obs) {
+      std::vector<double> res(2 * ((size_t)p->n_terms + 1));
+      rc = wide_expect(p, p->obs_codes.data(), p->n_terms + 1, res.data(), &S->wide_lane, &S->wide_ws);
+      if (!rc) energy = observable_value(p, res.data());
+    }
+    if (!rc && r->shots > 0) {
+      all.resize((size_t)r->shots * p->n);
+      rc = wide_sample(p, r->shots, r->seed, all.data(), &S->wide_lane, &S->wide_ws);
+    }
+    if (!rc) rc = prog_check_err(p);
+    {
+      std::lock_guard<std::mutex> lk(S->mu);
+      r->status = rc;
+      r->energy = energy;
+      if (!rc && r->shots > 0) select_measured(p, all.data(), r->shots, r->bits.data());
+      r->t_done = now_ms();
+      r->done = true;
+      S->inflight_bytes -= p->bytes;
+      S->inflight_reqs -= 1;
+      S->cv_done.notify_all();
+    }
+  }
+}
+
 }  // namespace gbmps
 
 using namespace gbmps;
@@ -193,9 +242,12 @@ int mps_serve_start(mps_ctx* c, int max_inflight) {
     if (e != cudaSuccess) return fail(MPS_ERR_CUDA, cudaGetErrorString(e));
     S->batches[l].lane = l;
   }
+  int rc = lane_init(S->wide_lane);
+  if (rc) return rc;
   S->running = true;
   c->serve = S;
   S->worker = std::thread(serve_loop, c);
+  S->wide_worker = std::thread(serve_wide_loop, c);
   return MPS_OK;
 }
 
@@ -203,7 +255,6 @@ int mps_serve_submit(mps_ctx* c, mps_prog* p, int shots, uint64_t seed, uint64_t
   if (!c || !p || !ticket || shots < 0) return fail(MPS_ERR_ARG, "bad argument");
   if (!c->serve) return fail(MPS_ERR_STATE, "serve loop not started");
   if (p->ctx != c) return fail(MPS_ERR_ARG, "program from another context");
-  if (prog_is_wide(p)) return fail(MPS_ERR_UNSUPPORTED, "the serve loop batches single-CTA programs (bond cap <= 64)");
   ServeState* S = c->serve;
   ServeReq* r = new ServeReq();
   r->prog = p;
@@ -224,8 +275,12 @@ int mps_serve_submit(mps_ctx* c, mps_prog* p, int shots, uint64_t seed, uint64_t
     }
     r->ticket = S->next_ticket++;
     S->all[r->ticket] = r;
-    S->queue.push_back(r);
+    if (prog_is_wide(p))
+      S->wide_queue.push_back(r);
+    else
+      S->queue.push_back(r);
   }
+  if (prog_is_wide(p)) S->cv_wide.notify_all();
   S->cv_work.notify_one();
   *ticket = r->ticket;
   return MPS_OK;
@@ -261,8 +316,12 @@ int mps_serve_stop(mps_ctx* c) {
     S->stop = true;
   }
   S->cv_work.notify_all();
+  S->cv_wide.notify_all();
   if (S->worker.joinable()) S->worker.join();
+  if (S->wide_worker.joinable()) S->wide_worker.join();
   cudaSetDevice(c->device);
+  lane_free(S->wide_lane);
+  wide_ws_free(&S->wide_ws);
   for (int l = 0; l < kServeLanes; ++l) {
     lane_free(S->lanes[l]);
     if (S->batches[l].ev) cudaEventDestroy(S->batches[l].ev);

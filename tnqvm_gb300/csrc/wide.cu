@@ -288,17 +288,21 @@ static void wide_bufs_free(WideBufs& B) {
   B = WideBufs();
 }
 
-void wide_free(mps_ctx* c) {
-  if (!c->wide) return;
-  WideAll* w = reinterpret_cast<WideAll*>(c->wide);
+void wide_ws_free(void** ws) {
+  if (!*ws) return;
+  WideAll* w = reinterpret_cast<WideAll*>(*ws);
   for (auto& b : w->b) wide_bufs_free(b);
   delete w;
-  c->wide = nullptr;
+  *ws = nullptr;
 }
 
-static int wide_bufs(mps_ctx* c, int prec, int chi, WideBufs** out) {
-  if (!c->wide) c->wide = new WideAll();
-  WideBufs& B = reinterpret_cast<WideAll*>(c->wide)->b[prec];
+void wide_free(mps_ctx* c) { wide_ws_free(&c->wide); }
+
+// Workspace `ws` (a WideAll, created on first use): the context's own, or
+// the serve loop's, so the two never share buffers.
+static int wide_bufs(void** ws, int prec, int chi, WideBufs** out) {
+  if (!*ws) *ws = new WideAll();
+  WideBufs& B = reinterpret_cast<WideAll*>(*ws)->b[prec];
   const int m = 2 * chi;
   if (B.prec == prec && B.m >= m) {
     *out = &B;
@@ -558,25 +562,29 @@ static int wide_gate2(mps_prog* p, WideBufs& B, cudaStream_t st, const DevOp& op
   // columns with zero weight are scaled by 0 (exatn) or never kept (itensor),
   // so only the first kk need to be orthonormal
   const int kk = std::max(1, std::min(k, kpos));
-  if (fp32 && kk < m) {
-    // one subspace step W <- X (X^H W) with X itself: the Gram's rounding
-    // tilts a kept eigenvector by ~eps * lambda_max / lambda, the product's
-    // only by ~eps * sigma_max / sigma
+  // FP32: one subspace step W <- X (X^H W) with X itself on the head columns
+  // (eigenvalues >= kRefine * lambda_max): the Gram's rounding tilts such an
+  // eigenvector by ~eps * lambda_max / lambda, the product's only by ~eps *
+  // sigma_max / sigma.  Tail columns come from the deflated Gram and are
+  // accurate to their own scale; the step would magnify their residual head
+  // components by lambda_head / lambda_tail.
+  const int ksub = fp32 ? std::min(kk, s_head) : 0;
+  if (ksub > 0 && ksub < m) {
     cx<T>* Y = reinterpret_cast<cx<T>*>(B.Y);
     cx<T>* W3 = reinterpret_cast<cx<T>*>(B.W3);
-    WCK(cgemm(adj(X), cmat<T>(Wk, m, kk, k, 1), cout_<T>(Y, nn, kk, kk, 1), T(1), T(0), B.gemm, st));
-    WCK(cgemm(X, cmat<T>(Y, nn, kk, kk, 1), cout_<T>(W3, m, kk, k, 1), T(1), T(0), B.gemm, st));
+    WCK(cgemm(adj(X), cmat<T>(Wk, m, ksub, k, 1), cout_<T>(Y, nn, ksub, ksub, 1), T(1), T(0), B.gemm, st));
+    WCK(cgemm(X, cmat<T>(Y, nn, ksub, ksub, 1), cout_<T>(W3, m, ksub, k, 1), T(1), T(0), B.gemm, st));
     T* inv = reinterpret_cast<T*>(B.scal) + 2 * B.m;
-    k_colnorm<T><<<(kk + 255) / 256, 256, 0, st>>>(W3, m, kk, k, Wk, k, inv);
-    k_colscale<T><<<blocks_for((int64_t)m * kk), 256, 0, st>>>(W3, m, kk, k, inv);
-    if (kk < k)  // zero-weight columns: carried over unchanged (scaled by 0 below)
-      WCK(cudaMemcpy2DAsync(W3 + kk, (size_t)k * sizeof(cx<T>), Wk + kk, (size_t)k * sizeof(cx<T>),
-                            (size_t)(k - kk) * sizeof(cx<T>), m, cudaMemcpyDeviceToDevice, st));
-    extra += 16.0 * m * nn * kk;
+    k_colnorm<T><<<(ksub + 255) / 256, 256, 0, st>>>(W3, m, ksub, k, Wk, k, inv);
+    k_colscale<T><<<blocks_for((int64_t)m * ksub), 256, 0, st>>>(W3, m, ksub, k, inv);
+    if (ksub < k)  // tail and zero-weight columns carried over unchanged
+      WCK(cudaMemcpy2DAsync(W3 + ksub, (size_t)k * sizeof(cx<T>), Wk + ksub, (size_t)k * sizeof(cx<T>),
+                            (size_t)(k - ksub) * sizeof(cx<T>), m, cudaMemcpyDeviceToDevice, st));
+    extra += 16.0 * m * nn * ksub;
     Wk = W3;
   }
   cx<T>* Wf = nullptr;
-  rc = orthonormalize_w<T>(B, X, m, nn, kk, k, Wk, true, st, &Wf, &extra);
+  rc = orthonormalize_w<T>(B, X, m, nn, kk, k, Wk, /*subspace=*/!refine, st, &Wf, &extra);
   if (rc) return rc;
   if (Wf != Wk && kk < k)
     WCK(cudaMemcpy2DAsync(Wf + kk, (size_t)k * sizeof(cx<T>), Wk + kk, (size_t)k * sizeof(cx<T>),
@@ -674,11 +682,11 @@ static int wide_run_t(mps_prog* p, WideBufs& B, cudaStream_t st, const std::vect
 
 bool prog_is_wide(const mps_prog* p) { return p->chi_cap > kChiLimit; }
 
-int wide_run(mps_ctx* c, Lane& L, mps_prog* p) {
+int wide_run(mps_ctx* c, Lane& L, mps_prog* p, void** ws) {
   std::vector<DevOp> ops;
   compile_program(p, ops);
   WideBufs* B = nullptr;
-  int rc = wide_bufs(c, p->prec, p->chi_cap, &B);
+  int rc = wide_bufs(ws ? ws : &c->wide, p->prec, p->chi_cap, &B);
   if (rc) return rc;
   rc = p->prec == MPS_PREC_FP64 ? wide_run_t<double>(p, *B, L.stream, ops) : wide_run_t<float>(p, *B, L.stream, ops);
   if (rc) return rc;
@@ -722,11 +730,11 @@ static int wide_expect_t(mps_prog* p, WideBufs& B, cudaStream_t st, const uint8_
   return MPS_OK;
 }
 
-int wide_expect(mps_prog* p, const uint8_t* codes, int n_terms, double* out) {
+int wide_expect(mps_prog* p, const uint8_t* codes, int n_terms, double* out, Lane* L, void** ws) {
   WideBufs* B = nullptr;
-  int rc = wide_bufs(p->ctx, p->prec, p->chi_cap, &B);
+  int rc = wide_bufs(ws ? ws : &p->ctx->wide, p->prec, p->chi_cap, &B);
   if (rc) return rc;
-  cudaStream_t st = p->ctx->lane0.stream;
+  cudaStream_t st = L ? L->stream : p->ctx->lane0.stream;
   return p->prec == MPS_PREC_FP64 ? wide_expect_t<double>(p, *B, st, codes, n_terms, out)
                                   : wide_expect_t<float>(p, *B, st, codes, n_terms, out);
 }
@@ -792,11 +800,11 @@ static int wide_sample_t(mps_prog* p, WideBufs& B, cudaStream_t st, int shots, u
   return rc;
 }
 
-int wide_sample(mps_prog* p, int shots, uint64_t seed, uint8_t* h_all_bits) {
+int wide_sample(mps_prog* p, int shots, uint64_t seed, uint8_t* h_all_bits, Lane* L, void** ws) {
   WideBufs* B = nullptr;
-  int rc = wide_bufs(p->ctx, p->prec, p->chi_cap, &B);
+  int rc = wide_bufs(ws ? ws : &p->ctx->wide, p->prec, p->chi_cap, &B);
   if (rc) return rc;
-  cudaStream_t st = p->ctx->lane0.stream;
+  cudaStream_t st = L ? L->stream : p->ctx->lane0.stream;
   return p->prec == MPS_PREC_FP64 ? wide_sample_t<double>(p, *B, st, shots, seed, h_all_bits)
                                   : wide_sample_t<float>(p, *B, st, shots, seed, h_all_bits);
 }
@@ -824,7 +832,7 @@ static int wide_amp_one_t(mps_prog* p, WideBufs& B, cudaStream_t st, const int* 
 
 int wide_amp_one(mps_prog* p, const int* bits, double* out) {
   WideBufs* B = nullptr;
-  int rc = wide_bufs(p->ctx, p->prec, p->chi_cap, &B);
+  int rc = wide_bufs(&p->ctx->wide, p->prec, p->chi_cap, &B);
   if (rc) return rc;
   cudaStream_t st = p->ctx->lane0.stream;
   return p->prec == MPS_PREC_FP64 ? wide_amp_one_t<double>(p, *B, st, bits, out)
@@ -846,7 +854,7 @@ int wide_diag_cgemm(mps_ctx* c, int M, int N, int K, const double* a, const doub
                     double* out_simt) {
   WideBufs* B = nullptr;
   const int chi = std::max(std::max(M, N), std::max(K, 64));
-  int rc = wide_bufs(c, MPS_PREC_FP32, (chi + 1) / 2 + 64, &B);
+  int rc = wide_bufs(&c->wide, MPS_PREC_FP32, (chi + 1) / 2 + 64, &B);
   if (rc) return rc;
   cudaStream_t st = c->lane0.stream;
   std::vector<cx<float>> ha((size_t)M * K), hb((size_t)K * N), hc((size_t)M * N);
