@@ -332,12 +332,99 @@ def extra_measurements(args, ctx, insts, energies, value):
                          "max_abs_dE_vs_batched": float(max(perr)) if perr else None}
     # serving latency: Poisson arrivals into the continuous-batching loop
     out["latency"] = serve_latency(args, ctx, insts, value)
+    # one large circuit on the wide path, and the mixed-cap serving stream
+    if args.wide:
+        out["wide_48q_chi512"] = wide_single(args, ctx)
+    if args.serve_mix > 0:
+        out["serve_mix"] = serve_mix(args, ctx)
     # CPU baseline (oracle port, all host threads)
     cv, cn, ct = cpu_sample(insts, args.cpu_budget)
     out["cpu_baseline"] = {"value": cv, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
                            "sample": "%d circuits of the batch (cost-stratified) in %.1f s; numpy complex128 "
                                      "MPS with LAPACK SVD (itensor-mode oracle)" % (cn, ct)}
     return out
+
+
+def wide_single(args, ctx):
+    """48-qubit brick wall, depth 30 (U3 + CZ), bond cap 512, cutoff 1e-10:
+    one circuit on the wide path in complex64 (tcgen05 3xTF32 products, FP32
+    eigensolver with deflation refinement), canonical truncation with the
+    gates of each layer swept in centre order (MPS_FLAG_SWEEP); outputs
+    <Z_i Z_i+1> for all i and the truncation fidelity; with --wide-ref also
+    the complex128 run at the same cap and the error against it."""
+    from tnqvm_gb300 import circuits
+    from tnqvm_gb300 import mps as M
+    n, depth, chi, cut = 48, 30, 512, 1e-10
+    circ = circuits.brickwall(n, depth, seed=2, entangler="CZ")
+    terms = ["I" * i + "ZZ" + "I" * (n - i - 2) for i in range(n - 1)]
+    out = {"workload": "brickwall n=48 depth=30 U3+CZ, chi<=512, cutoff 1e-10, itensor truncation, swept gate order"}
+    vals = {}
+    for prec in ([M.PREC_FP32, M.PREC_FP64] if args.wide_ref else [M.PREC_FP32]):
+        tc0, _ = ctx.gemm_counts()
+        t0 = time.perf_counter()
+        p = M.Program(ctx, n, chi, cut, M.TRUNC_ITENSOR, prec, M.FLAG_SWEEP)
+        p.run(circ)
+        p.submit()
+        p.wait()
+        t1 = time.perf_counter()
+        v = p.expect_pauli(terms).real / p.norm()
+        st = p.stats()
+        tc1, _ = ctx.gemm_counts()
+        key = "c64" if prec == M.PREC_FP32 else "c128"
+        vals[key] = v
+        out[key] = {"seconds": t1 - t0, "circuits_per_s": 1.0 / (t1 - t0), "splits": st["gate2"], "ops": st["ops"],
+                    "max_bond": max(p.bond_dims()), "truncation_fidelity": float(st["fidelity"]),
+                    "tensor_core_gemms": tc1 - tc0}
+        p.close()
+    if "c128" in vals:
+        d = np.abs(vals["c64"] - vals["c128"])
+        out["err_c64_vs_c128"] = {"max_abs_dZZ": float(d.max()), "median_abs_dZZ": float(np.median(d))}
+    return out
+
+
+def serve_mix(args, ctx):
+    """Poisson arrivals of random brick-wall circuits (qubits U{10..64},
+    depth U{10..40}, bond cap from {16, 64, 256, 512}), each returning 1024
+    shots and one Pauli expectation, through the continuous-batching loop
+    (caps above 64 on its wide lane)."""
+    from tnqvm_gb300 import circuits
+    from tnqvm_gb300 import mps as M
+    rng = np.random.default_rng(44)
+    reqs = []
+    for i in range(args.serve_mix):
+        n = int(rng.integers(10, 65))
+        depth = int(rng.integers(10, 41))
+        chi = int(rng.choice([16, 64, 256, 512]))
+        p = M.Program(ctx, n, chi, 1e-10, M.TRUNC_ITENSOR, M.PREC_FP32)
+        p.run(circuits.brickwall(n, depth, seed=1000 + i))
+        s = "".join(rng.choice(list("IXYZ"), n))
+        p.set_observable([s], [1.0])
+        reqs.append((p, chi))
+    ctx.serve_start(256)
+    lats = {16: [], 64: [], 256: [], 512: []}
+    try:
+        gaps = rng.exponential(1.0 / args.serve_mix_rate, len(reqs))
+        tickets = []
+        t0 = time.perf_counter()
+        t_next = t0
+        for (p, chi), gap in zip(reqs, gaps):
+            t_next += gap
+            while time.perf_counter() < t_next:
+                pass
+            tickets.append(ctx.serve_submit(p, 1024, 7))
+        for (p, chi), t in zip(reqs, tickets):
+            _, _, lat = ctx.serve_poll(t, p, 1024)
+            lats[chi].append(lat)
+        wall = time.perf_counter() - t0
+    finally:
+        ctx.serve_stop()
+        for p, _ in reqs:
+            p.close()
+    allv = [x for v in lats.values() for x in v]
+    return {"requests": len(reqs), "offered_rate_per_s": args.serve_mix_rate, "circuits_per_s": len(reqs) / wall,
+            "p50_ms": float(np.percentile(allv, 50)), "p99_ms": float(np.percentile(allv, 99)),
+            "p50_ms_by_cap": {str(k): float(np.percentile(v, 50)) for k, v in lats.items() if v},
+            "mode": "qubits U{10..64}, depth U{10..40}, cap {16,64,256,512}, 1024 shots + 1 Pauli term each"}
 
 
 def serve_latency(args, ctx, insts, value):
@@ -392,6 +479,10 @@ def main():
     ap.add_argument("--ref-sample", type=int, default=4)
     ap.add_argument("--serve-requests", type=int, default=256)
     ap.add_argument("--no-extras", action="store_true")
+    ap.add_argument("--wide", type=int, default=1, help="time the 48-qubit chi=512 circuit (1/0)")
+    ap.add_argument("--wide-ref", action="store_true", help="also run it in complex128 and report the error")
+    ap.add_argument("--serve-mix", type=int, default=0, help="requests of the mixed-cap serving stream (0: off)")
+    ap.add_argument("--serve-mix-rate", type=float, default=100.0)
     ap.add_argument("--qmax", type=int, default=32, help="largest qubit count (small profiling cases)")
     ap.add_argument("--lmax", type=int, default=12, help="largest layer count (small profiling cases)")
     args = ap.parse_args()

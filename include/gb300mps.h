@@ -50,6 +50,9 @@ extern "C" {
 /* program flags */
 #define MPS_FLAG_RENORM 1   /* rescale the kept part to the pre-truncation norm */
 #define MPS_FLAG_PER_GATE 2 /* one kernel launch per gate (the plain visitor path) */
+#define MPS_FLAG_SWEEP 4    /* itensor semantics: reorder gates on disjoint qubits so the
+                               orthogonality centre takes the shortest path (no reference
+                               counterpart; truncations then happen in another order) */
 
 /* largest bond dimension the single-CTA gate kernel handles */
 #define MPS_CHI_LIMIT 64

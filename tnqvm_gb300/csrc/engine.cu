@@ -134,6 +134,64 @@ void compile_program(mps_prog* p, std::vector<DevOp>& ops) {
     raw.push_back(r);
   }
 
+  // Sweep scheduling (itensor semantics, opt-in): gates on disjoint qubits
+  // commute, so among the gates whose predecessors on both sites are done,
+  // take the one nearest the orthogonality centre (ties: the direction of
+  // travel).  A brick-wall layer then costs one centre move per gate instead
+  // of a sweep back across the chain after every layer.  The state is the
+  // same up to the order in which truncations happen.
+  if (p->mode == MPS_TRUNC_ITENSOR && (p->flags & MPS_FLAG_SWEEP) && raw.size() > 1) {
+    const int n = p->n;
+    std::vector<std::vector<int>> per(n);
+    for (size_t i = 0; i < raw.size(); ++i) {
+      per[raw[i].site].push_back((int)i);
+      if (raw[i].kind == OP_GATE2) per[raw[i].site + 1].push_back((int)i);
+    }
+    std::vector<size_t> head(n, 0);
+    auto ready = [&](int i) {
+      const Raw& r = raw[i];
+      if (per[r.site][head[r.site]] != i) return false;
+      return r.kind != OP_GATE2 || per[r.site + 1][head[r.site + 1]] == i;
+    };
+    std::vector<Raw> order;
+    order.reserve(raw.size());
+    int c = p->center, dir = 1;
+    std::vector<char> done(raw.size(), 0);
+    std::vector<int> cand;
+    for (size_t step = 0; step < raw.size(); ++step) {
+      cand.clear();
+      for (int q = 0; q < n; ++q)
+        if (head[q] < per[q].size()) {
+          const int i = per[q][head[q]];
+          if (!done[i] && raw[i].site == q && ready(i)) cand.push_back(i);
+        }
+      int best = -1;
+      long long bkey = 0;
+      for (int i : cand) {
+        const Raw& r = raw[i];
+        const int lo = r.site, hi = r.kind == OP_GATE2 ? lo + 1 : lo;
+        const int dist = c < lo ? lo - c : (c > hi ? c - hi : 0);
+        const int side = (lo >= c) == (dir > 0) ? 0 : 1;
+        const long long key = (long long)dist * 4 + side * 2 + (r.kind == OP_GATE2 ? 0 : 1);
+        if (best < 0 || key < bkey || (key == bkey && i < best)) {
+          best = i;
+          bkey = key;
+        }
+      }
+      const Raw& r = raw[best];
+      done[best] = 1;
+      ++head[r.site];
+      if (r.kind == OP_GATE2) {
+        ++head[r.site + 1];
+        const int target = c < r.site ? r.site : (c > r.site + 1 ? r.site + 1 : c);
+        if (target != c) dir = target > c ? 1 : -1;
+        c = target;
+      }
+      order.push_back(r);
+    }
+    raw.swap(order);
+  }
+
   auto emit = [&](int kind, int site, int orient, const cd* m, int nm) {
     DevOp o;
     std::memset(&o, 0, sizeof(o));

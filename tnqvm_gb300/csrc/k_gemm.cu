@@ -438,8 +438,9 @@ cudaError_t cgemm(const CMat<float>& A, const CMat<float>& B, const CMatOut<floa
                   GemmWs& ws, cudaStream_t st) {
   const int M = C.rows, N = C.cols, K = A.cols;
   if (M <= 0 || N <= 0) return cudaSuccess;
-  // small products (less than one tile in M or N) stay on the CUDA cores
-  if (M < 128 || N < 64 || K < 16 || !get_encode()) {
+  // small products (under ~2M complex MACs, or too thin to fill a tile
+  // pair) stay on the CUDA cores; the rest are padded to 128 x 128 tiles
+  if ((double)M * N * K < 2097152.0 || N < 16 || K < 16 || !get_encode()) {
     ++ws.simt_launches;
     return simt_launch<float>(A, B, C, alpha, beta, st);
   }

@@ -80,8 +80,8 @@ void gemm_ws_free(GemmWs& ws);
 
 // C = alpha * A * B + beta * C with A (M x K), B (K x N), C (M x N) views.
 // complex64 runs on tcgen05 (3xTF32: hi*hi + hi*lo + lo*hi, FP32
-// accumulation in tensor memory) when the product fills at least one
-// 128 x 64 tile, else on CUDA cores; complex128 runs on CUDA cores.
+// accumulation in tensor memory) for products of at least ~2M complex MACs,
+// else on CUDA cores; complex128 runs on CUDA cores.
 cudaError_t cgemm(const CMat<float>& A, const CMat<float>& B, const CMatOut<float>& C, float alpha, float beta,
                   GemmWs& ws, cudaStream_t st);
 cudaError_t cgemm(const CMat<double>& A, const CMat<double>& B, const CMatOut<double>& C, double alpha,

@@ -16,7 +16,7 @@ LIB_PATH = os.path.join(_HERE, "_lib", "libgb300mps.so")
 OK, ERR_ARG, ERR_OOM, ERR_TIMEOUT, ERR_NUMERIC, ERR_CUDA, ERR_STATE, ERR_UNSUPPORTED = range(8)
 TRUNC_EXATN, TRUNC_ITENSOR = 0, 1
 PREC_FP64, PREC_FP32 = 0, 1
-FLAG_RENORM, FLAG_PER_GATE = 1, 2
+FLAG_RENORM, FLAG_PER_GATE, FLAG_SWEEP = 1, 2, 4
 CHI_LIMIT = 64
 WIDE_CHI_LIMIT = 1024
 
