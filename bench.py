@@ -279,7 +279,7 @@ def run_ours(args):
                          "peak_source": "%s bf16 dense, sustained" % pk_kind,
                          "flops_per_launch": gemm_flops, "kernel_ms": ops_ms,
                          "eigensolver_flops_per_launch": eig_flops,
-                         "note": "GEMM-class flops only (theta merge, gate, Gram, split); the Jacobi "
+                         "note": "GEMM-class flops only (theta merge, gate, Gram, split); the tridiagonal "
                                  "eigensolver runs on FP32 CUDA cores and dominates the kernel time"},
             "phases_ms": {"reset_plus_ops": ops_ms, "observables": exp_ms},
             "fused_kernel_cycle_share": phase_share,

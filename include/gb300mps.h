@@ -163,7 +163,7 @@ int mps_graph_stream(mps_graph* g, void** cuda_stream);
 /* Device time of the last replay from CUDA events captured in the graph:
  * out[0] reset + fused op kernel, out[1] observables (+ copy), in ms; out[2]
  * algorithmic GEMM-class flops of the op kernel (theta merge + gate + Gram +
- * split, eigensolver excluded), out[3] eigensolver rotation flops, out[4]
+ * split, eigensolver excluded), out[3] eigensolver (Householder) flops, out[4]
  * bytes of the op table copied to the device by mps_graph_update, out[5]
  * bytes copied back per replay. */
 int mps_graph_timing(mps_graph* g, double out[6]);

@@ -10,11 +10,12 @@
 // one launch with no inter-CTA waits.
 //
 // Two-site split: theta = gate . (A . B) is formed in per-CTA scratch, its
-// Gram matrix on the isometric side is diagonalised by a parallel cyclic
-// Jacobi method (round-robin pairs, all m/2 rotations of a step applied at
-// once as 2x2 block updates), the eigenvalues (squared singular values) are
-// sorted, the kept dimension is chosen with FP64 sums, and the other side is
-// the projection W_k^H X (no division by singular values).
+// Gram matrix on the isometric side is reduced to real tridiagonal form by
+// Householder reflections, every eigenvalue (squared singular value) is found
+// by multisection bisection and ranked, the kept dimension is chosen with
+// FP64 sums, the kept eigenvectors come from twisted factorisations and the
+// back-transform, and the other side is the projection W_k^H X (no division
+// by singular values).
 #include <math.h>
 
 #include <cstring>
@@ -228,7 +229,7 @@ __device__ void householder_qr(cx<T>* M, int mr, int nc, cx<T>* Rb, SmallSmem<T>
 }
 
 // ------------------------------------------------- tridiagonal eigensolver
-// FP32 path of the Gram eigen-decomposition, ~10x fewer flops than Jacobi:
+// Gram eigen-decomposition (both precisions), ~10x fewer flops than Jacobi:
 // Householder reduction to real symmetric tridiagonal form, eigenvalues of
 // each unreduced block by multisection bisection (Sturm counts), the kept
 // eigenvectors by one twisted factorisation each (Dhillon-Parlett), and the
