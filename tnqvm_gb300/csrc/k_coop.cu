@@ -193,12 +193,12 @@ __device__ EigWork<T> eig_work(void* base, int m, int grid) {
   return e;
 }
 
-// Shared memory: [td te (T) | bs bt (int) | union: 3 vectors of m / W block
+// Shared memory: [td te (T) | bs bt (int) | union: 4 vectors of m / W block
 // (m x cb) / m doubles | reduction scratch]
 template <typename T>
 __host__ __device__ inline size_t eig_smem_bytes(int m) {
   const size_t head = al256(2 * m * sizeof(T)) + al256(2 * m * sizeof(int));
-  size_t u = 3 * (size_t)m * sizeof(cx<T>);
+  size_t u = 4 * (size_t)m * sizeof(cx<T>);
   const size_t wb = (size_t)m * CoopPrec<T>::cb * sizeof(cx<T>);
   if (wb > u) u = wb;
   if ((size_t)m * sizeof(double) > u) u = (size_t)m * sizeof(double);
@@ -279,7 +279,7 @@ __global__ void __launch_bounds__(kCoopThreads, 1) k_wide_eig(WideEigArgs a) {
   int* sbs = reinterpret_cast<int*>(smem + al256(2 * m * sizeof(T)));
   int* sbt = sbs + m;
   unsigned char* uni = smem + al256(2 * m * sizeof(T)) + al256(2 * m * sizeof(int));
-  size_t usz = 3 * (size_t)m * sizeof(cx<T>);
+  size_t usz = 4 * (size_t)m * sizeof(cx<T>);
   {
     const size_t wb = (size_t)m * CoopPrec<T>::cb * sizeof(cx<T>);
     if (wb > usz) usz = wb;
@@ -300,17 +300,50 @@ __global__ void __launch_bounds__(kCoopThreads, 1) k_wide_eig(WideEigArgs a) {
   const T flush2 = T(CoopPrec<T>::tri_flush * trace * trace + CoopPrec<T>::tiny);
   for (int i = cta + G * tid; i < m; i += G * nt) stcg(wk.colbuf + i, A[(int64_t)i * m]);
   if (!grid_sync(wk.bar)) return;
+  // After the barrier of step j-1 every CTA needs p_{j-1} (to form w_{j-1})
+  // and column j's buffer; both were written before that barrier, so their
+  // loads are issued together (one L2 round trip per column).
+  cx<T>* craw = vcur + m;  // column j as the owners wrote it (before step j-1's update)
   bool hasprev = false;
+  cx<T> tau_prev = mk<T>(T(0), T(0));
   for (int j = 0; j + 1 < m; ++j) {
     const int buf = j & 1;
     const cx<T>* cb_in = wk.colbuf + buf * m;
     cx<T>* cb_out = wk.colbuf + (buf ^ 1) * m;
+    if (hasprev) {
+      // (d) of step j-1: w = p - 1/2 tau (p^H v) v
+      const int pb = buf ^ 1;
+      if (warp == 0) {
+        // fixed summation order: lane-strided partial sums, then a butterfly
+        cx<T> d = mk<T>(T(0), T(0));
+        for (int q = lane; q < G; q += 32) d = d + ldcg(wk.part + pb * G + q);
+        for (int o = 16; o > 0; o >>= 1) {
+          d.re += __shfl_xor_sync(0xffffffffu, d.re, o);
+          d.im += __shfl_xor_sync(0xffffffffu, d.im, o);
+        }
+        if (lane == 0) redc[0] = d;
+      }
+      for (int i = j + tid; i < m; i += nt) {
+        wprev[i] = ldcg(wk.pvec + pb * m + i);
+        craw[i] = ldcg(cb_in + i);
+      }
+      __syncthreads();
+      const cx<T> a2 = scl(tau_prev * redc[0], T(-0.5));
+      for (int i = j + tid; i < m; i += nt) {
+        const cx<T> v = vcur[i];
+        wprev[i] = wprev[i] + a2 * v;
+        vprev[i] = v;
+      }
+    } else {
+      for (int i = j + tid; i < m; i += nt) craw[i] = ldcg(cb_in + i);
+    }
+    __syncthreads();
     // (a) column j of the current matrix (rows j..m-1), kept in vcur
     const cx<T> cwj = hasprev ? conj(wprev[j]) : mk<T>(T(0), T(0));
     const cx<T> cvj = hasprev ? conj(vprev[j]) : mk<T>(T(0), T(0));
     T s_part = T(0);
     for (int i = j + tid; i < m; i += nt) {
-      cx<T> c = ldcg(cb_in + i);
+      cx<T> c = craw[i];
       if (hasprev) c = c - (vprev[i] * cwj + wprev[i] * cvj);
       vcur[i] = c;
       if (i >= j + 2) s_part += abs2(c);
@@ -384,31 +417,20 @@ __global__ void __launch_bounds__(kCoopThreads, 1) k_wide_eig(WideEigArgs a) {
     const cx<T> dsum_cta = coop_sum_c<T>(dpart, redc);
     if (tid == 0) stcg(wk.part + buf * G + cta, dsum_cta);
     if (!grid_sync(wk.bar)) return;
-    // (d) w = p - 1/2 tau (p^H v) v for the next step
-    if (warp == 0) {
-      // fixed summation order: lane-strided partial sums, then a butterfly
-      cx<T> d = mk<T>(T(0), T(0));
-      for (int q = lane; q < G; q += 32) d = d + ldcg(wk.part + buf * G + q);
-      for (int o = 16; o > 0; o >>= 1) {
-        d.re += __shfl_xor_sync(0xffffffffu, d.re, o);
-        d.im += __shfl_xor_sync(0xffffffffu, d.im, o);
-      }
-      if (lane == 0) redc[0] = d;
-    }
-    __syncthreads();
-    const cx<T> dsum = redc[0];
-    const cx<T> a2 = scl(tau * dsum, T(-0.5));
     hasprev = refl;
-    for (int i = j + 1 + tid; i < m; i += nt) {
-      const cx<T> v = vcur[i];
-      wprev[i] = ldcg(wk.pvec + buf * m + i) + a2 * v;
-      vprev[i] = v;
-    }
-    __syncthreads();
+    tau_prev = tau;
   }
   if (cta == 0 && tid == 0) {
+    // last diagonal entry: column m-1's buffer minus step m-2's rank-2 term
     cx<T> c = ldcg(wk.colbuf + ((m - 1) & 1) * m + (m - 1));
-    if (hasprev) c = c - (vprev[m - 1] * conj(wprev[m - 1]) + wprev[m - 1] * conj(vprev[m - 1]));
+    if (hasprev) {
+      const int pb = (m - 2) & 1;
+      cx<T> d = mk<T>(T(0), T(0));
+      for (int q = 0; q < G; ++q) d = d + ldcg(wk.part + pb * G + q);
+      const cx<T> v = vcur[m - 1];
+      const cx<T> w = ldcg(wk.pvec + pb * m + (m - 1)) + scl(tau_prev * d, T(-0.5)) * v;
+      c = c - (v * conj(w) + w * conj(v));
+    }
     wk.td[m - 1] = c.re;
     wk.te[m - 1] = T(0);
     if (m == 1) wk.ttau[0] = mk<T>(T(0), T(0));
@@ -513,7 +535,7 @@ __global__ void __launch_bounds__(kCoopThreads, 1) k_wide_eigvec(WideEigArgs a) 
   int* sbs = reinterpret_cast<int*>(smem + al256(2 * m * sizeof(T)));
   int* sbt = sbs + m;
   unsigned char* uni = smem + al256(2 * m * sizeof(T)) + al256(2 * m * sizeof(int));
-  size_t usz = 3 * (size_t)m * sizeof(cx<T>);
+  size_t usz = 4 * (size_t)m * sizeof(cx<T>);
   {
     const size_t wb = (size_t)m * CoopPrec<T>::cb * sizeof(cx<T>);
     if (wb > usz) usz = wb;
@@ -634,6 +656,7 @@ struct QrArgsT {
   CMat<T> M;        // input view mr x nc
   CMatOut<T> Q;     // output view mr x k (element (i, c) = Q(i, c), conjugated if qconj)
   int qconj;
+  int own_smem;     // the CTA's own columns live in shared memory during the factorisation
   cx<T>* R;         // k x nc row-major
   void* work;
   int* err;
@@ -662,14 +685,35 @@ __device__ void grid_tile_copy(int nr, int nc, bool lanes_on_rows, Src src, Dst 
   }
 }
 
+// Dynamic shared memory of k_wide_qr: 32 x 33 tile, reduction scratch, two
+// staged reflectors (2 x mr), then (own_smem) the CTA's own columns.
+template <typename T>
+__host__ __device__ inline size_t qr_smem_bytes(int mr, int nown, bool own) {
+  return al256(sizeof(cx<T>) * 32 * 33) + 256 + al256(2 * (size_t)mr * sizeof(cx<T>)) +
+         (own ? (size_t)nown * mr * sizeof(cx<T>) : 0);
+}
+
 template <typename T>
 __global__ void __launch_bounds__(kCoopThreads, 1) k_wide_qr(QrArgsT<T> a) {
-  __shared__ cx<T> tile[32][33];
-  __shared__ cx<T> s_red[kCoopWarps];
-  __shared__ T s_sum[kCoopWarps];
+  extern __shared__ __align__(16) unsigned char qsm[];
   const int mr = a.M.rows, nc = a.M.cols, k = mr < nc ? mr : nc;
   const int G = gridDim.x, cta = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   QrWork<T> wk = qr_work<T>(a.work, mr, nc);
+  cx<T>(*tile)[33] = reinterpret_cast<cx<T>(*)[33]>(qsm);
+  T* s_sum = reinterpret_cast<T*>(qsm + al256(sizeof(cx<T>) * 32 * 33));
+  cx<T>* vbuf = reinterpret_cast<cx<T>*>(qsm + al256(sizeof(cx<T>) * 32 * 33) + 256);
+  cx<T>* own = vbuf + 2 * (size_t)mr;
+  const bool osm = a.own_smem != 0;
+  const int nown = cta < nc ? (nc - cta + G - 1) / G : 0;
+  // own column li (global index cta + G li): shared memory, or its row of MT
+  auto col = [&](int li) -> cx<T>* { return osm ? own + (size_t)li * mr : wk.MT + (int64_t)(cta + G * li) * mr; };
+  auto ld = [&](const cx<T>* p) { return osm ? *p : ldcg(p); };
+  auto st = [&](cx<T>* p, cx<T> z) {
+    if (osm)
+      *p = z;
+    else
+      stcg(p, z);
+  };
   // 0. MT[c][i] = M(i, c)
   {
     const CMat<T> M = a.M;
@@ -683,16 +727,22 @@ __global__ void __launch_bounds__(kCoopThreads, 1) k_wide_qr(QrArgsT<T> a) {
     grid_tile_copy<T>(mr, nc, M.rs == 1, src, dst, tile);
   }
   if (!grid_sync(wk.bar)) return;
+  if (osm)
+    for (int li = 0; li < nown; ++li)
+      for (int i = tid; i < mr; i += kCoopThreads) own[(size_t)li * mr + i] = ldcg(wk.MT + (int64_t)(cta + G * li) * mr + i);
+  __syncthreads();
   const T tiny = T(CoopPrec<T>::tiny);
   // 1. reflectors; column c is owned by CTA c % G, one warp per owned column
   for (int j = 0; j < k; ++j) {
     if (j % G == cta) {
-      // the whole owner CTA forms reflector j (block-wide norm)
-      cx<T>* x = wk.MT + (int64_t)j * mr;  // own column (written by other CTAs in step 0: read via L2)
+      // the whole owner CTA forms reflector j (block-wide norm) and
+      // publishes it in MT (row j) for the other CTAs
+      cx<T>* x = col(j / G);
+      cx<T>* xg = wk.MT + (int64_t)j * mr;
       T s_part = T(0);
-      for (int i = j + 1 + tid; i < mr; i += kCoopThreads) s_part += abs2(ldcg(x + i));
+      for (int i = j + 1 + tid; i < mr; i += kCoopThreads) s_part += abs2(ld(x + i));
       const T s = coop_sum<T>(s_part, s_sum);
-      const cx<T> alpha = ldcg(x + j);
+      const cx<T> alpha = ld(x + j);
       const T ar = alpha.re, ai = alpha.im;
       const T nrm2 = ar * ar + ai * ai + s;
       const bool refl = !(s == T(0) && ai == T(0)) && nrm2 > tiny;
@@ -703,11 +753,16 @@ __global__ void __launch_bounds__(kCoopThreads, 1) k_wide_qr(QrArgsT<T> a) {
         const T ir = dr / den, ii = -di / den;
         tau = mk<T>((beta - ar) / beta, -ai / beta);
         for (int i = j + 1 + tid; i < mr; i += kCoopThreads) {
-          const cx<T> v = ldcg(x + i);
-          stcg(x + i, mk<T>(v.re * ir - v.im * ii, v.re * ii + v.im * ir));
+          const cx<T> v = ld(x + i);
+          const cx<T> sv = mk<T>(v.re * ir - v.im * ii, v.re * ii + v.im * ir);
+          st(x + i, sv);
+          if (osm) stcg(xg + i, sv);
         }
         __syncthreads();  // every thread has read alpha
-        if (tid == 0) stcg(x + j, mk<T>(beta, T(0)));
+        if (tid == 0) {
+          st(x + j, mk<T>(beta, T(0)));
+          if (osm) stcg(xg + j, mk<T>(beta, T(0)));
+        }
       }
       if (tid == 0) stcg(wk.tau + j, tau);
     }
@@ -716,25 +771,30 @@ __global__ void __launch_bounds__(kCoopThreads, 1) k_wide_qr(QrArgsT<T> a) {
     if (tj.re == T(0) && tj.im == T(0)) continue;
     const cx<T> ctau = conj(tj);
     const cx<T>* v = wk.MT + (int64_t)j * mr;
-    for (int li = warp;; li += kCoopWarps) {
+    for (int i = j + 1 + tid; i < mr; i += kCoopThreads) vbuf[i] = ldcg(v + i);
+    __syncthreads();
+    for (int li = warp; li < nown; li += kCoopWarps) {
       const int c = cta + G * li;
-      if (c >= nc) break;
       if (c <= j) continue;
-      cx<T>* y = wk.MT + (int64_t)c * mr;
+      cx<T>* y = col(li);
       cx<T> w = mk<T>(T(0), T(0));
-      for (int i = j + 1 + lane; i < mr; i += 32) fma_cj(w, ldcg(v + i), ldcg(y + i));
+      for (int i = j + 1 + lane; i < mr; i += 32) fma_cj(w, vbuf[i], ld(y + i));
       for (int o = 16; o > 0; o >>= 1) {
         w.re += __shfl_xor_sync(0xffffffffu, w.re, o);
         w.im += __shfl_xor_sync(0xffffffffu, w.im, o);
       }
-      w = w + ldcg(y + j);
+      w = w + ld(y + j);
       const cx<T> tw = ctau * w;
-      for (int i = j + 1 + lane; i < mr; i += 32) stcg(y + i, ldcg(y + i) - ldcg(v + i) * tw);
+      for (int i = j + 1 + lane; i < mr; i += 32) st(y + i, ld(y + i) - vbuf[i] * tw);
       __syncwarp();
-      if (lane == 0) stcg(y + j, ldcg(y + j) - tw);
+      if (lane == 0) st(y + j, ld(y + j) - tw);
       __syncwarp();
     }
     __syncthreads();  // column j+1 is final before its owner forms the next reflector
+  }
+  if (osm) {
+    for (int li = 0; li < nown; ++li)
+      for (int i = tid; i < mr; i += kCoopThreads) stcg(wk.MT + (int64_t)(cta + G * li) * mr + i, own[(size_t)li * mr + i]);
   }
   if (!grid_sync(wk.bar)) return;
   // 2. R (k x nc): R[r][c] = MT[c][r] for r <= c
@@ -755,32 +815,58 @@ __global__ void __launch_bounds__(kCoopThreads, 1) k_wide_qr(QrArgsT<T> a) {
       __syncthreads();
     }
   }
-  // 3. Q columns: q_c = H_0 ... H_c e_c, one warp per column
-  for (int li = warp;; li += kCoopWarps) {
-    const int c = cta + G * li;
-    if (c >= k) break;
-    cx<T>* q = wk.QT + (int64_t)c * mr;
-    for (int i = lane; i < mr; i += 32) q[i] = mk<T>(T(i == c), T(0));
-    __syncwarp();
-    for (int j = c; j >= 0; --j) {
-      const cx<T> tj = ldcg(wk.tau + j);
-      if (tj.re == T(0) && tj.im == T(0)) continue;
-      const cx<T>* v = wk.MT + (int64_t)j * mr;
-      cx<T> w = mk<T>(T(0), T(0));
-      for (int i = j + 1 + lane; i < mr; i += 32) fma_cj(w, ldcg(v + i), q[i]);
-      for (int o = 16; o > 0; o >>= 1) {
-        w.re += __shfl_xor_sync(0xffffffffu, w.re, o);
-        w.im += __shfl_xor_sync(0xffffffffu, w.im, o);
+  // 3. Q columns: q_c = H_0 ... H_c e_c.  The CTA walks the reflectors from
+  // its largest own column down to 0, each staged once in shared memory for
+  // all its warps (double-buffered, the next one's loads issued before this
+  // one's products); one warp per own column.
+  const int nq = cta < k ? (k - cta + G - 1) / G : 0;
+  for (int li = warp; li < nq; li += kCoopWarps) {
+    cx<T>* q = wk.QT + (int64_t)(cta + G * li) * mr;
+    for (int i = lane; i < mr; i += 32) q[i] = mk<T>(T(i == cta + G * li), T(0));
+  }
+  if (nq > 0) {
+    const int cmax = cta + G * (nq - 1);
+    constexpr int PF = 8;  // staged elements per thread (mr <= 2048)
+    cx<T> pre[PF];
+    auto fetch = [&](int j) {
+#pragma unroll
+      for (int u = 0; u < PF; ++u) {
+        const int i = j + 1 + tid + u * kCoopThreads;
+        pre[u] = i < mr ? ldcg(wk.MT + (int64_t)j * mr + i) : mk<T>(T(0), T(0));
       }
-      w = w + q[j];
-      const cx<T> tw = tj * w;
-      for (int i = j + 1 + lane; i < mr; i += 32) q[i] = q[i] - ldcg(v + i) * tw;
-      __syncwarp();
-      if (lane == 0) q[j] = q[j] - tw;
-      __syncwarp();
+    };
+    fetch(cmax);
+    for (int j = cmax; j >= 0; --j) {
+      cx<T>* vb = vbuf + (size_t)(j & 1) * mr;
+#pragma unroll
+      for (int u = 0; u < PF; ++u) {
+        const int i = j + 1 + tid + u * kCoopThreads;
+        if (i < mr) vb[i] = pre[u];
+      }
+      for (int i = j + 1 + PF * kCoopThreads + tid; i < mr; i += kCoopThreads) vb[i] = ldcg(wk.MT + (int64_t)j * mr + i);
+      const cx<T> tj = ldcg(wk.tau + j);
+      __syncthreads();
+      if (j > 0) fetch(j - 1);
+      if (tj.re == T(0) && tj.im == T(0)) continue;
+      for (int li = warp; li < nq; li += kCoopWarps) {
+        const int c = cta + G * li;
+        if (c < j) continue;
+        cx<T>* q = wk.QT + (int64_t)c * mr;
+        cx<T> w = mk<T>(T(0), T(0));
+        for (int i = j + 1 + lane; i < mr; i += 32) fma_cj(w, vb[i], q[i]);
+        for (int o = 16; o > 0; o >>= 1) {
+          w.re += __shfl_xor_sync(0xffffffffu, w.re, o);
+          w.im += __shfl_xor_sync(0xffffffffu, w.im, o);
+        }
+        w = w + q[j];
+        const cx<T> tw = tj * w;
+        for (int i = j + 1 + lane; i < mr; i += 32) q[i] = q[i] - vb[i] * tw;
+        __syncwarp();
+        if (lane == 0) q[j] = q[j] - tw;
+        __syncwarp();
+      }
     }
   }
-  (void)s_red;
   if (!grid_sync(wk.bar)) return;
   // 4. Q out through the output view
   {
@@ -859,6 +945,13 @@ cudaError_t launch_wide_eig(int prec, const WideEigArgs& a, int grid, cudaStream
 template <typename T>
 cudaError_t launch_wide_qr_t(const CMat<T>& M, const CMatOut<T>& Q, int qconj, void* R, void* work, int* err,
                              int grid, cudaStream_t st) {
+  static bool attr = false;
+  constexpr size_t kQrSmemMax = 200 * 1024;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(k_wide_qr<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kQrSmemMax);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
   cudaError_t e = cudaMemsetAsync(work, 0, 256, st);
   if (e != cudaSuccess) return e;
   QrArgsT<T> a;
@@ -868,8 +961,12 @@ cudaError_t launch_wide_qr_t(const CMat<T>& M, const CMatOut<T>& Q, int qconj, v
   a.R = reinterpret_cast<cx<T>*>(R);
   a.work = work;
   a.err = err;
+  const int nown = (M.cols + grid - 1) / grid;
+  size_t sm = qr_smem_bytes<T>(M.rows, nown, true);
+  a.own_smem = sm <= kQrSmemMax ? 1 : 0;
+  if (!a.own_smem) sm = qr_smem_bytes<T>(M.rows, nown, false);
   void* params[] = {&a};
-  return cudaLaunchCooperativeKernel((const void*)k_wide_qr<T>, dim3(grid), dim3(kCoopThreads), params, 0, st);
+  return cudaLaunchCooperativeKernel((const void*)k_wide_qr<T>, dim3(grid), dim3(kCoopThreads), params, sm, st);
 }
 template cudaError_t launch_wide_qr_t<float>(const CMat<float>&, const CMatOut<float>&, int, void*, void*, int*,
                                              int, cudaStream_t);

@@ -350,6 +350,15 @@ static int wide_bufs(void** ws, int prec, int chi, WideBufs** out) {
 
 static int blocks_for(int64_t n) { return (int)std::min<int64_t>((n + 255) / 256, 4096); }
 
+// Grid of a cooperative launch over n rows (eigensolver) or columns (QR):
+// about one per warp, at most the co-resident maximum.  Fewer CTAs make each
+// grid barrier cheaper when the matrix is small.
+static int coop_grid_for(int prec, int which, int n) {
+  const int g = coop_grid(prec, which);
+  const int want = std::max(8, (n + 7) / 8);
+  return std::min(g, want);
+}
+
 // ------------------------------------------------------------ two-site update
 template <typename T>
 static int orthonormalize_w(WideBufs& B, const CMat<T>& X, int m, int nn, int kk, int ld, cx<T>* Wc, bool subspace,
@@ -385,7 +394,7 @@ static int orthonormalize_w(WideBufs& B, const CMat<T>& X, int m, int nn, int kk
   if (qr_taken) {
     // degenerate cluster: Householder QR, then (when vectors were completed
     // from rounding noise) one subspace step with X and a second QR
-    const int grid = coop_grid(sizeof(T) == 8 ? 0 : 1, 1);
+    const int grid = coop_grid_for(sizeof(T) == 8 ? 0 : 1, 1, kk);
     for (int pass = 0; pass < 2; ++pass) {
       WCK(launch_wide_qr_t<T>(view(cur), oview(nxt), 0, B.R, B.qr_work, B.d_err, grid, st));
       std::swap(cur, nxt);
@@ -420,7 +429,7 @@ static int eig_values(WideBufs& B, void* G, void* work, int m, double* h_lam, cu
   ea.phase = 0;
   ea.work = work;
   ea.status_err = B.d_status;
-  WCK(launch_wide_eig(prec, ea, coop_grid(prec, 0), st));
+  WCK(launch_wide_eig(prec, ea, coop_grid_for(prec, 0, m), st));
   int* herr = reinterpret_cast<int*>(B.h_pinned + 64);
   WCK(cudaMemcpyAsync(h_lam, B.lam, sizeof(double) * m, cudaMemcpyDeviceToHost, st));
   WCK(cudaMemcpyAsync(herr, B.d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -445,7 +454,7 @@ static int eig_vectors(WideBufs& B, void* G, void* work, int m, int kv, void* W,
   ea.ld = ld;
   ea.work = work;
   ea.status_err = B.d_status;
-  WCK(launch_wide_eig(prec, ea, coop_grid(prec, 0), st));
+  WCK(launch_wide_eig(prec, ea, coop_grid_for(prec, 0, m), st));
   return MPS_OK;
 }
 
@@ -625,12 +634,12 @@ static int wide_move(mps_prog* p, WideBufs& B, cudaStream_t st, const DevOp& op)
   const int c = op.site;
   cx<T>* sites = reinterpret_cast<cx<T>*>(p->d_sites);
   const int prec = sizeof(T) == 8 ? 0 : 1;
-  const int grid = coop_grid(prec, 1);
   cx<T>* tmp = reinterpret_cast<cx<T>*>(B.tbuf);
   cx<T>* Rm = reinterpret_cast<cx<T>*>(B.R);
   if (op.kind == OP_MOVE_R) {
     const int dl = p->hbond[c], dr = p->hbond[c + 1], d2 = p->hbond[c + 2];
     const int mr = 2 * dl, k = std::min(mr, dr);
+    const int grid = coop_grid_for(prec, 1, dr);
     cx<T>* Ac = sites + p->off[c];
     cx<T>* An = sites + p->off[c + 1];
     WCK(launch_wide_qr_t<T>(cmat<T>(Ac, mr, dr, dr, 1), cout_<T>(Ac, mr, k, k, 1), 0, Rm, B.qr_work, B.d_err, grid,
@@ -643,6 +652,7 @@ static int wide_move(mps_prog* p, WideBufs& B, cudaStream_t st, const DevOp& op)
   } else {
     const int dl = p->hbond[c], dr = p->hbond[c + 1], d0 = p->hbond[c - 1];
     const int mr = 2 * dr, k = std::min(mr, dl);
+    const int grid = coop_grid_for(prec, 1, dl);
     cx<T>* Ac = sites + p->off[c];
     cx<T>* Ap = sites + p->off[c - 1];
     // M = A_c^H: M(i, j) = conj(A_c[j][i]) with A_c as dl x 2dr
