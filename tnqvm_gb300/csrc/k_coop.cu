@@ -194,12 +194,12 @@ __device__ EigWork<T> eig_work(void* base, int m, int grid) {
 }
 
 // Shared memory: [td te (T) | bs bt (int) | union: 4 vectors of m / W block
-// (m x cb) / m doubles | reduction scratch]
+// (m x cb) and a staged reflector / m doubles | reduction scratch]
 template <typename T>
 __host__ __device__ inline size_t eig_smem_bytes(int m) {
   const size_t head = al256(2 * m * sizeof(T)) + al256(2 * m * sizeof(int));
   size_t u = 4 * (size_t)m * sizeof(cx<T>);
-  const size_t wb = (size_t)m * CoopPrec<T>::cb * sizeof(cx<T>);
+  const size_t wb = (size_t)m * (CoopPrec<T>::cb + 1) * sizeof(cx<T>);
   if (wb > u) u = wb;
   if ((size_t)m * sizeof(double) > u) u = (size_t)m * sizeof(double);
   return head + al256(u) + 4096;
@@ -281,7 +281,7 @@ __global__ void __launch_bounds__(kCoopThreads, 1) k_wide_eig(WideEigArgs a) {
   unsigned char* uni = smem + al256(2 * m * sizeof(T)) + al256(2 * m * sizeof(int));
   size_t usz = 4 * (size_t)m * sizeof(cx<T>);
   {
-    const size_t wb = (size_t)m * CoopPrec<T>::cb * sizeof(cx<T>);
+    const size_t wb = (size_t)m * (CoopPrec<T>::cb + 1) * sizeof(cx<T>);
     if (wb > usz) usz = wb;
     if ((size_t)m * sizeof(double) > usz) usz = (size_t)m * sizeof(double);
   }
@@ -537,7 +537,7 @@ __global__ void __launch_bounds__(kCoopThreads, 1) k_wide_eigvec(WideEigArgs a) 
   unsigned char* uni = smem + al256(2 * m * sizeof(T)) + al256(2 * m * sizeof(int));
   size_t usz = 4 * (size_t)m * sizeof(cx<T>);
   {
-    const size_t wb = (size_t)m * CoopPrec<T>::cb * sizeof(cx<T>);
+    const size_t wb = (size_t)m * (CoopPrec<T>::cb + 1) * sizeof(cx<T>);
     if (wb > usz) usz = wb;
     if ((size_t)m * sizeof(double) > usz) usz = (size_t)m * sizeof(double);
   }
@@ -579,6 +579,7 @@ __global__ void __launch_bounds__(kCoopThreads, 1) k_wide_eigvec(WideEigArgs a) 
   constexpr int CB = CoopPrec<T>::cb;
   constexpr int Q = kCoopThreads / CB;  // row chunks
   cx<T>* Ws = reinterpret_cast<cx<T>*>(uni);
+  cx<T>* vb = Ws + (size_t)m * CB;                      // staged reflector (m entries)
   cx<T>* part = reinterpret_cast<cx<T>*>(redb + 1024);  // per-warp partial sums (CB each)
   const int ngroups = (k + CB - 1) / CB;
   for (int g = cta; g < ngroups; g += G) {
@@ -589,13 +590,36 @@ __global__ void __launch_bounds__(kCoopThreads, 1) k_wide_eigvec(WideEigArgs a) 
     }
     __syncthreads();
     const int c = tid % CB, q = tid / CB;
-    for (int j = m - 2; j >= 0; --j) {
-      const cx<T> tj = ldcg(wk.ttau + j);
-      if (tj.re == T(0) && tj.im == T(0)) continue;
+    // reflector j (row j of A, v[0] = 1 stored) staged in vb for all threads;
+    // the next one's loads are issued before this one's products
+    constexpr int PF = kWideM / kCoopThreads;
+    cx<T> pre[PF];
+    auto fetch = [&](int j) {
+      const cx<T>* v = A + (int64_t)j * m + (j + 1);
       const int L = m - j - 1;
-      const cx<T>* v = A + (int64_t)j * m + (j + 1);  // v[0] = 1 stored
+#pragma unroll
+      for (int u = 0; u < PF; ++u) {
+        const int i = tid + u * kCoopThreads;
+        pre[u] = i < L ? ldcg(v + i) : mk<T>(T(0), T(0));
+      }
+    };
+    if (m >= 2) fetch(m - 2);
+    for (int j = m - 2; j >= 0; --j) {
+      const int L = m - j - 1;
+#pragma unroll
+      for (int u = 0; u < PF; ++u) {
+        const int i = tid + u * kCoopThreads;
+        if (i < L) vb[i] = pre[u];
+      }
+      const cx<T> tj = ldcg(wk.ttau + j);
+      __syncthreads();
+      if (j > 0) fetch(j - 1);
+      if (tj.re == T(0) && tj.im == T(0)) {
+        __syncthreads();  // vb is rewritten next
+        continue;
+      }
       cx<T> acc = mk<T>(T(0), T(0));
-      for (int r = q; r < L; r += Q) fma_cj(acc, ldcg(v + r), Ws[(j + 1 + r) * CB + c]);
+      for (int r = q; r < L; r += Q) fma_cj(acc, vb[r], Ws[(j + 1 + r) * CB + c]);
       // reduce over the Q row chunks: lanes q, q+32/CB, ... share c within a warp
       for (int o = 16; o >= CB; o >>= 1) {
         acc.re += __shfl_xor_sync(0xffffffffu, acc.re, o);
@@ -608,7 +632,7 @@ __global__ void __launch_bounds__(kCoopThreads, 1) k_wide_eigvec(WideEigArgs a) 
       sc = tj * sc;
       for (int r = q; r < L; r += Q) {
         cx<T>& x = Ws[(j + 1 + r) * CB + c];
-        x = x - ldcg(v + r) * sc;
+        x = x - vb[r] * sc;
       }
       __syncthreads();
     }

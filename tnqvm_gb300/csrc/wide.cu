@@ -361,10 +361,13 @@ static int coop_grid_for(int prec, int which, int n) {
 
 // ------------------------------------------------------------ two-site update
 template <typename T>
-static int orthonormalize_w(WideBufs& B, const CMat<T>& X, int m, int nn, int kk, int ld, cx<T>* Wc, bool subspace,
+static int orthonormalize_w(WideBufs& B, const CMat<T>& X, int m, int nn, int kk, int ld, cx<T>* Wc, int nsub,
                             cudaStream_t st, cx<T>** result, double* ortho_flops) {
   // Wc: m x kk (row stride ld).  Returns the orthonormal columns in *result
   // (m x kk, row stride ld); columns kk..ld-1 of the result are unspecified.
+  // nsub: leading columns whose eigenvalue lies clearly above the Gram's
+  // rounding floor; after a QR fallback only they take the subspace step
+  // (a column at the floor must stay in X's null space).
   cx<T>* cur = Wc;
   cx<T>* nxt = reinterpret_cast<cx<T>*>(cur == B.W3 ? B.W2 : B.W3);
   cx<T>* S = reinterpret_cast<cx<T>*>(B.S);
@@ -373,23 +376,32 @@ static int orthonormalize_w(WideBufs& B, const CMat<T>& X, int m, int nn, int kk
   bool qr_taken = false;
   auto view = [&](cx<T>* p) { return cmat<T>(p, m, kk, ld, 1); };
   auto oview = [&](cx<T>* p) { return cout_<T>(p, m, kk, ld, 1); };
-  for (int it = 0; it < 5; ++it) {
-    WCK(cgemm(adj(view(cur)), view(cur), cout_<T>(S, kk, kk, kk, 1), T(1), T(0), B.gemm, st));
-    *ortho_flops += 8.0 * kk * kk * m;
-    k_defect<T><<<1, 256, 0, st>>>(S, kk, B.d_scalar);
-    WCK(cudaMemcpyAsync(hs, B.d_scalar, sizeof(double), cudaMemcpyDeviceToHost, st));
-    WCK(cudaStreamSynchronize(st));
-    const double fro = hs[0];
-    if (!(fro == fro)) return fail(MPS_ERR_NUMERIC, "non-finite value in a wide split");
-    if (it == 0 && fro > 0.1) {
-      qr_taken = true;
-      break;
+  // The defect |W^H W - I|_F is read back once; each Newton-Schulz step
+  // W <- W (3 I - W^H W) / 2 maps a defect e to at most 3/4 e^2 + 1/4 e^3,
+  // so the number of steps follows from it without further round trips
+  // (steps until the one taken from a defect below ns_stop, at most five).
+  WCK(cgemm(adj(view(cur)), view(cur), cout_<T>(S, kk, kk, kk, 1), T(1), T(0), B.gemm, st));
+  *ortho_flops += 8.0 * kk * kk * m;
+  k_defect<T><<<1, 256, 0, st>>>(S, kk, B.d_scalar);
+  WCK(cudaMemcpyAsync(hs, B.d_scalar, sizeof(double), cudaMemcpyDeviceToHost, st));
+  WCK(cudaStreamSynchronize(st));
+  double fro = hs[0];
+  if (!(fro == fro)) return fail(MPS_ERR_NUMERIC, "non-finite value in a wide split");
+  if (fro > 0.1) {
+    qr_taken = true;
+  } else {
+    for (int it = 0; it < 5; ++it) {
+      if (it > 0) {
+        WCK(cgemm(adj(view(cur)), view(cur), cout_<T>(S, kk, kk, kk, 1), T(1), T(0), B.gemm, st));
+        *ortho_flops += 8.0 * kk * kk * m;
+      }
+      WCK(cudaMemcpyAsync(nxt, cur, (size_t)m * ld * sizeof(cx<T>), cudaMemcpyDeviceToDevice, st));
+      WCK(cgemm(view(cur), cmat<T>(S, kk, kk, kk, 1), oview(nxt), T(-0.5), T(1.5), B.gemm, st));
+      *ortho_flops += 8.0 * kk * kk * m;
+      std::swap(cur, nxt);
+      if (fro < ns_stop) break;
+      fro = 0.75 * fro * fro + 0.25 * fro * fro * fro;
     }
-    WCK(cudaMemcpyAsync(nxt, cur, (size_t)m * ld * sizeof(cx<T>), cudaMemcpyDeviceToDevice, st));
-    WCK(cgemm(view(cur), cmat<T>(S, kk, kk, kk, 1), oview(nxt), T(-0.5), T(1.5), B.gemm, st));
-    *ortho_flops += 8.0 * kk * kk * m;
-    std::swap(cur, nxt);
-    if (fro < ns_stop) break;
   }
   if (qr_taken) {
     // degenerate cluster: Householder QR, then (when vectors were completed
@@ -398,19 +410,22 @@ static int orthonormalize_w(WideBufs& B, const CMat<T>& X, int m, int nn, int kk
     for (int pass = 0; pass < 2; ++pass) {
       WCK(launch_wide_qr_t<T>(view(cur), oview(nxt), 0, B.R, B.qr_work, B.d_err, grid, st));
       std::swap(cur, nxt);
-      if (pass == 1 || kk >= m || !subspace) break;
+      const int ns = std::min(nsub, kk);
+      if (pass == 1 || kk >= m || ns <= 0) break;
       cx<T>* Y = reinterpret_cast<cx<T>*>(B.Y);
-      WCK(cgemm(adj(X), view(cur), cout_<T>(Y, nn, kk, kk, 1), T(1), T(0), B.gemm, st));
-      WCK(cgemm(X, cmat<T>(Y, nn, kk, kk, 1), oview(nxt), T(1), T(0), B.gemm, st));
+      WCK(cgemm(adj(X), cmat<T>(cur, m, ns, ld, 1), cout_<T>(Y, nn, ns, ns, 1), T(1), T(0), B.gemm, st));
+      WCK(cudaMemcpyAsync(nxt, cur, (size_t)m * ld * sizeof(cx<T>), cudaMemcpyDeviceToDevice, st));
+      WCK(cgemm(X, cmat<T>(Y, nn, ns, ns, 1), cout_<T>(nxt, m, ns, ld, 1), T(1), T(0), B.gemm, st));
       T* inv = reinterpret_cast<T*>(B.scal) + 2 * B.m;
-      k_colnorm<T><<<(kk + 255) / 256, 256, 0, st>>>(nxt, m, kk, ld, cur, ld, inv);
-      k_colscale<T><<<blocks_for((int64_t)m * kk), 256, 0, st>>>(nxt, m, kk, ld, inv);
+      k_colnorm<T><<<(ns + 255) / 256, 256, 0, st>>>(nxt, m, ns, ld, cur, ld, inv);
+      k_colscale<T><<<blocks_for((int64_t)m * ns), 256, 0, st>>>(nxt, m, ns, ld, inv);
       std::swap(cur, nxt);
-      *ortho_flops += 16.0 * m * nn * kk;
+      *ortho_flops += 16.0 * m * nn * ns;
     }
-    int herr = 0;
-    WCK(cudaMemcpy(&herr, B.d_err, sizeof(int), cudaMemcpyDeviceToHost));
-    if (herr) return fail(MPS_ERR_TIMEOUT, "cooperative QR gave up at a grid barrier");
+    int* herr = reinterpret_cast<int*>(B.h_pinned + 96);
+    WCK(cudaMemcpyAsync(herr, B.d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    WCK(cudaStreamSynchronize(st));
+    if (*herr) return fail(MPS_ERR_TIMEOUT, "cooperative QR gave up at a grid barrier");
   }
   *result = cur;
   return MPS_OK;
@@ -509,8 +524,7 @@ static int wide_gate2(mps_prog* p, WideBufs& B, cudaStream_t st, const DevOp& op
     rc = eig_vectors<T>(B, G, B.eig_work, m, s_head, Wh, s_head, st);
     if (rc) return rc;
     cx<T>* Who = nullptr;
-    rc = orthonormalize_w<T>(B, X, m, nn, s_head, s_head, Wh == reinterpret_cast<cx<T>*>(B.W3) ? Wh : Wh, false, st,
-                             &Who, &extra);
+    rc = orthonormalize_w<T>(B, X, m, nn, s_head, s_head, Wh, 0, st, &Who, &extra);
     if (rc) return rc;
     // keep W_h in B.W (the buffers W2/W3 serve the orthonormalisation)
     if (Who != Wh)
@@ -592,8 +606,16 @@ static int wide_gate2(mps_prog* p, WideBufs& B, cudaStream_t st, const DevOp& op
     extra += 16.0 * m * nn * ksub;
     Wk = W3;
   }
+  // columns eligible for a subspace step after a QR fallback: eigenvalue
+  // above the Gram's rounding floor (FP32: the head; FP64: 1e-10 lambda_max)
+  int nsub = 0;
+  if (fp32) {
+    nsub = refine ? 0 : std::min(kk, s_head);
+  } else {
+    while (nsub < kk && lk[nsub] >= 1e-10 * lk[0]) ++nsub;
+  }
   cx<T>* Wf = nullptr;
-  rc = orthonormalize_w<T>(B, X, m, nn, kk, k, Wk, /*subspace=*/!refine, st, &Wf, &extra);
+  rc = orthonormalize_w<T>(B, X, m, nn, kk, k, Wk, nsub, st, &Wf, &extra);
   if (rc) return rc;
   if (Wf != Wk && kk < k)
     WCK(cudaMemcpy2DAsync(Wf + kk, (size_t)k * sizeof(cx<T>), Wk + kk, (size_t)k * sizeof(cx<T>),
@@ -619,10 +641,10 @@ static int wide_gate2(mps_prog* p, WideBufs& B, cudaStream_t st, const DevOp& op
   k_wide_commit<<<1, 1, 0, st>>>(p->d_stats, p->d_bond, lo + 1, k, total, kept, flops, eig_flops);
   WCK(cudaGetLastError());
   // the host buffer hk must outlive the copy above
+  int* herr = reinterpret_cast<int*>(B.h_pinned + 64);
+  WCK(cudaMemcpyAsync(herr, B.d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
   WCK(cudaStreamSynchronize(st));
-  int herr = 0;
-  WCK(cudaMemcpy(&herr, B.d_status, sizeof(int), cudaMemcpyDeviceToHost));
-  if (herr) return fail(MPS_ERR_TIMEOUT, "cooperative eigensolver gave up at a grid barrier");
+  if (*herr) return fail(MPS_ERR_TIMEOUT, "cooperative eigensolver gave up at a grid barrier");
   p->hbond[lo + 1] = k;
   return MPS_OK;
 }
@@ -687,6 +709,13 @@ static int wide_run_t(mps_prog* p, WideBufs& B, cudaStream_t st, const std::vect
     }
     if (rc) return rc;
   }
+  // time-out flags of the QR moves and of the tensor-core GEMMs
+  int* hf = reinterpret_cast<int*>(B.h_pinned + 100);
+  WCK(cudaMemcpyAsync(hf, B.d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+  WCK(cudaMemcpyAsync(hf + 1, B.gemm.d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+  WCK(cudaStreamSynchronize(st));
+  if (hf[0]) return fail(MPS_ERR_TIMEOUT, "cooperative QR gave up at a grid barrier");
+  if (hf[1]) return fail(MPS_ERR_TIMEOUT, "tensor-core GEMM gave up waiting on its pipeline");
   return MPS_OK;
 }
 
