@@ -202,3 +202,24 @@ def test_sweep_schedule_exact(ctx, chi):
             assert np.max(np.abs(amp - psi)) < TOL64
             ops[flags] = p.stats()["ops"]
     assert ops[M.FLAG_SWEEP] < ops[0]
+
+
+def test_wide_itensor_fixtures_where_cap_is_loose(ctx):
+    """The vendored-ITensor fixtures whose bond cap never binds (every bond
+    below the cap) run as wide programs (cap 128): the same bond dimensions
+    and <P> within 1e-10 as ITensor v3 (tests/golden/itensor_fixtures.json)."""
+    import json
+    import os
+    fx = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "itensor_fixtures.json")))
+    used = 0
+    for c in fx["cases"]:
+        if max(c["bonds"]) >= c["chi"]:
+            continue
+        used += 1
+        circ = [(g, tuple(q), tuple(p)) for g, q, p in c["circuit"]]
+        with run(ctx, c["n"], circ, 128, c["cutoff"], M.TRUNC_ITENSOR, M.PREC_FP64) as p:
+            assert p.bond_dims() == c["bonds"], c["name"]
+            vals = p.expect_pauli(c["paulis"])
+            for s, v, want in zip(c["paulis"], vals, c["expect"]):
+                assert abs(v - complex(*want)) < TOL64, (c["name"], s)
+    assert used >= 3

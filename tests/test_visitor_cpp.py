@@ -55,3 +55,15 @@ def test_plugin_sampling_and_itensor_mode():
     psi = dense.run(3, g)
     out = _run(3, 0, g, [("precision", "fp32")])
     assert abs(out["norm"] - np.sum(np.abs(psi) ** 2)) < 1e-6
+
+
+@pytest.mark.gpu
+def test_plugin_wide_bond_cap():
+    """max-bond-dim above 64 through the plugin: the splits run on the wide
+    path; exp-val-z and the norm match the dense oracle."""
+    n = 14
+    circ = circuits.brickwall(n, 12, seed=6) + [("Measure", (q,), ()) for q in (1, 6, 12)]
+    psi = dense.run(n, circ)
+    out = _run(n, 0, circ, [("max-bond-dim", 128), ("svd-cutoff", 1e-14)])
+    assert abs(out["norm"] - 1.0) < 1e-10
+    assert abs(out["exp-val-z"] - dense.expect_z_parity(psi, [1, 6, 12])) < 1e-10
