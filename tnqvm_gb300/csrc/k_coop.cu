@@ -20,7 +20,7 @@
 // columns owned cyclically by the CTAs, one grid barrier per column.
 //
 // All CTAs of a launch are co-resident (cooperative launch, grid <= SMs x
-// occupancy).  The grid barrier is a counter/generation pair with a 2 s
+// occupancy).  The grid barrier is a monotonic arrival counter with a 2 s
 // bound on every wait: a CTA that gives up sets kCoopTimeout and all CTAs
 // leave the kernel at their next barrier.  Data written by other CTAs during
 // the launch is read with ld.global.cg (L2), never through L1.
@@ -55,10 +55,10 @@ constexpr int kCoopWarps = kCoopThreads / 32;
 constexpr long long kBarrierNs = 2000000000LL;
 
 struct GridBar {
-  unsigned int count;
-  unsigned int gen;
+  unsigned int count;  // arrivals so far (zeroed before each launch)
+  unsigned int pad;
   int err;
-  int k;  // kept dimension, broadcast by CTA 0
+  int k;
 };
 
 __device__ __forceinline__ long long coop_timer() {
@@ -80,37 +80,41 @@ __device__ __forceinline__ void stcg(cx<T>* p, cx<T> z) {
   __stcg(&p->im, z.im);
 }
 
-// Grid-wide barrier with a bounded wait.  Returns false when any CTA timed
-// out (the caller leaves the kernel).
+// Grid-wide barrier with a bounded wait.  The counter only grows: a CTA's
+// arrival (release atomic) returns the count before it, which fixes the
+// barrier's epoch and the count that marks everyone's arrival; the CTA then
+// spins on acquire loads of the counter until it reaches that mark (later
+// barriers only raise it further).  Every 256 polls it checks the 2 s bound
+// and the error word another CTA may have set.  Returns false when any CTA
+// timed out (the caller leaves the kernel).
 __device__ bool grid_sync(GridBar* b) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
     int ok = 1;
-    volatile unsigned int* vgen = &b->gen;
-    const unsigned int g = *vgen;
-    __threadfence();
-    const unsigned int arrived = atomicAdd(&b->count, 1u);
-    if (arrived == gridDim.x - 1) {
-      atomicExch(&b->count, 0u);
-      __threadfence();
-      atomicAdd(&b->gen, 1u);
-    } else {
-      const long long t0 = coop_timer();
-      while (*vgen == g) {
+    unsigned int old;
+    asm volatile("atom.add.release.gpu.global.u32 %0, [%1], 1;" : "=r"(old) : "l"(&b->count) : "memory");
+    const unsigned int G = gridDim.x;
+    const unsigned int target = (old / G + 1u) * G;
+    unsigned int cur = old + 1u;
+    long long t0 = -1;
+    for (unsigned int polls = 1; cur < target; ++polls) {
+      asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(cur) : "l"(&b->count) : "memory");
+      if ((polls & 255u) == 0u) {
         if (*(volatile int*)&b->err) {
           ok = 0;
           break;
         }
-        if (coop_timer() - t0 > kBarrierNs) {
+        const long long t = coop_timer();
+        if (t0 < 0) {
+          t0 = t;
+        } else if (t - t0 > kBarrierNs) {
           atomicOr(&b->err, kCoopTimeout);
           ok = 0;
           break;
         }
-        __nanosleep(32);
       }
     }
-    __threadfence();
     s_ok = ok && *(volatile int*)&b->err == 0;
   }
   __syncthreads();
