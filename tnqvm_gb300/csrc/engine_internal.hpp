@@ -85,6 +85,8 @@ struct ServeBatch {
   std::vector<std::pair<ServeReq*, uint8_t*>> bit_dst;
   uint8_t* h_bits = nullptr;   // pinned
   size_t h_bits_cap = 0;
+  int* h_err = nullptr;        // pinned: each request's error word, copied behind the batch
+  size_t h_err_cap = 0;
   size_t footprint = 0;
 };
 

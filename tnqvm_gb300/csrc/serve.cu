@@ -9,6 +9,7 @@
 // different lanes overlap on the device, so requests that arrive while others
 // run start as soon as a lane is free instead of waiting for the running
 // batch to drain.  Completed requests are finished out of order.
+#include <algorithm>
 #include <chrono>
 #include <cstring>
 
@@ -17,7 +18,10 @@
 
 namespace gbmps {
 
-constexpr int kServeLanes = 4;
+// Lanes whose batches overlap on the device.  One circuit runs per CTA, so
+// a batch fills the GPU only with ~150 circuits; more lanes let the small
+// batches that steady arrivals produce run side by side instead of queueing.
+constexpr int kServeLanes = 16;
 
 static double now_ms() {
   return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
@@ -41,9 +45,13 @@ static void finish_batch(ServeState* S, ServeBatch& B) {
   const double t = now_ms();
   std::lock_guard<std::mutex> lk(S->mu);
   size_t ti = 0;
+  size_t ri = 0;
   for (ServeReq* r : B.reqs) {
     mps_prog* p = r->prog;
-    r->status = prog_check_err(p);
+    const int herr = B.h_err[ri++];
+    r->status = (herr & ERR_NAN)    ? fail(MPS_ERR_NUMERIC, "non-finite value in a two-site split")
+                : (herr & ERR_DIMS) ? fail(MPS_ERR_UNSUPPORTED, "bond dimension beyond the kernel limit")
+                                    : MPS_OK;
     if (p->d_obs) {
       r->energy = observable_value(p, B.h_exp + 2 * ti);
       ti += (size_t)p->n_terms + 1;
@@ -98,6 +106,13 @@ static int launch_batch(mps_ctx* c, ServeState* S, int li, std::vector<ServeReq*
       B.bit_dst.push_back({r, B.h_bits + off});
       off += (size_t)r->shots * r->prog->n;
     }
+  }
+  // error words of the batch's programs, read by finish_batch without a sync
+  rc = grow_pinned((void**)&B.h_err, &B.h_err_cap, reqs.size() * sizeof(int));
+  if (rc) return rc;
+  for (size_t i = 0; i < reqs.size(); ++i) {
+    cudaError_t e = cudaMemcpyAsync(B.h_err + i, reqs[i]->prog->d_err, sizeof(int), cudaMemcpyDeviceToHost, L.stream);
+    if (e != cudaSuccess) return fail(MPS_ERR_CUDA, cudaGetErrorString(e));
   }
   cudaError_t e = cudaEventRecord(B.ev, L.stream);
   if (e != cudaSuccess) return fail(MPS_ERR_CUDA, cudaGetErrorString(e));
@@ -327,6 +342,7 @@ int mps_serve_stop(mps_ctx* c) {
     if (S->batches[l].ev) cudaEventDestroy(S->batches[l].ev);
     if (S->batches[l].h_exp) cudaFreeHost(S->batches[l].h_exp);
     if (S->batches[l].h_bits) cudaFreeHost(S->batches[l].h_bits);
+    if (S->batches[l].h_err) cudaFreeHost(S->batches[l].h_err);
   }
   for (auto& kv : S->all) delete kv.second;
   delete S;
