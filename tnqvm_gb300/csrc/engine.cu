@@ -305,8 +305,10 @@ int launch_programs(mps_ctx* c, Lane& L, mps_prog* const* progs_in, int n_in, bo
     compile_program(progs[i], all[i]);
     total += all[i].size();
   }
+  bool any_fused = false;
+  for (int i = 0; i < n; ++i) any_fused = any_fused || progs[i]->serve_flag != nullptr;
   cudaError_t e;
-  if (total > 0) {
+  if (total > 0 || any_fused) {
     std::vector<DevOp> flat;
     flat.reserve(total);
     std::vector<size_t> first(n);
@@ -314,7 +316,10 @@ int launch_programs(mps_ctx* c, Lane& L, mps_prog* const* progs_in, int n_in, bo
       first[i] = flat.size();
       flat.insert(flat.end(), all[i].begin(), all[i].end());
     }
-    int rc = grow(&L.d_ops, &L.d_ops_cap, flat.size());
+    // generous first sizes: growing a buffer reallocates, and device
+    // allocation synchronises the whole device (lanes of the serve loop run
+    // side by side)
+    int rc = grow(&L.d_ops, &L.d_ops_cap, std::max<size_t>(flat.size(), 65536));
     if (rc) return rc;
     std::vector<ProgDesc> descs;
     auto make_desc = [&](int i, size_t off, int nops) {
@@ -333,6 +338,12 @@ int launch_programs(mps_ctx* c, Lane& L, mps_prog* const* progs_in, int n_in, bo
       d.cutoff = p->cutoff;
       d.stats = p->d_stats;
       d.err = p->d_err;
+      if (p->serve_flag) {
+        d.obs_codes = p->d_obs;
+        d.n_obs = p->d_obs ? p->n_terms + 1 : 0;
+        d.obs_out = p->serve_obs;
+        d.done = p->serve_flag;
+      }
       return d;
     };
     if (per_gate) {
@@ -346,12 +357,14 @@ int launch_programs(mps_ctx* c, Lane& L, mps_prog* const* progs_in, int n_in, bo
         order[i] = i;
         const double cap = (double)progs[i]->chi_cap;
         for (const DevOp& o : all[i]) cost[i] += (o.kind == OP_GATE2 ? 1.0 : 0.1) * cap * cap * cap;
+        if (progs[i]->serve_flag && progs[i]->d_obs)  // fused observables: ~a tenth of a split per site and term
+          cost[i] += 0.1 * (progs[i]->n_terms + 1) * progs[i]->n * cap * cap * cap;
       }
       std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[a] > cost[b]; });
       for (int i : order)
-        if (!all[i].empty()) descs.push_back(make_desc(i, first[i], (int)all[i].size()));
+        if (!all[i].empty() || progs[i]->serve_flag) descs.push_back(make_desc(i, first[i], (int)all[i].size()));
     }
-    rc = grow(&L.d_desc, &L.d_desc_cap, descs.size());
+    rc = grow(&L.d_desc, &L.d_desc_cap, std::max<size_t>(descs.size(), 1024));
     if (rc) return rc;
     // pageable sources: the call returns once the data is staged, so the
     // vectors may be released right after
@@ -369,7 +382,7 @@ int launch_programs(mps_ctx* c, Lane& L, mps_prog* const* progs_in, int n_in, bo
       }
     } else {
       const int grid = std::min(nd, c->num_sms);
-      rc = ensure_bytes(&L.op_scratch[prec], &L.op_scratch_ctas[prec], grid, op_scratch_bytes(prec));
+      rc = ensure_bytes(&L.op_scratch[prec], &L.op_scratch_ctas[prec], c->num_sms, op_scratch_bytes(prec));
       if (rc) return rc;
       e = cudaMemsetAsync(L.d_queue, 0, sizeof(int), L.stream);
       if (e != cudaSuccess) return fail(MPS_ERR_CUDA, cudaGetErrorString(e));

@@ -73,6 +73,13 @@ struct ServeReq {
   double energy;
   std::vector<uint8_t> bits;
   bool done;
+  // fused completion: observables evaluated by the program's own CTA, results
+  // and a done flag in the batch's host-mapped arena
+  bool fused = false;
+  int* flag = nullptr;       // [0] done, [1] error word
+  double* obs = nullptr;     // 2 * (n_terms + 1) doubles
+  bool in_batch = false;     // still referenced by a running batch
+  bool reaped = false;       // polled by the client while in_batch
 };
 
 struct ServeBatch {
@@ -87,6 +94,8 @@ struct ServeBatch {
   size_t h_bits_cap = 0;
   int* h_err = nullptr;        // pinned: each request's error word, copied behind the batch
   size_t h_err_cap = 0;
+  char* arena = nullptr;       // pinned, mapped: fused requests' flags and observables
+  size_t arena_cap = 0;
   size_t footprint = 0;
 };
 
@@ -150,6 +159,10 @@ struct mps_prog {
   std::vector<uint8_t> obs_codes;  // host copy of the observable (wide programs)
   int n_terms = 0;
   std::vector<int> hbond;  // host mirror of the bond dimensions (wide programs)
+  // set by the serve loop for one launch: evaluate the observable in the
+  // update kernel and signal completion through host-mapped memory
+  double* serve_obs = nullptr;
+  int* serve_flag = nullptr;
 };
 
 namespace gbmps {

@@ -22,6 +22,7 @@
 #include <mutex>
 #include <string>
 
+#include "expect_sweep.cuh"
 #include "keep.cuh"
 #include "mps_common.cuh"
 
@@ -1124,6 +1125,34 @@ k_run_ops(const ProgDesc* __restrict__ progs, int n_progs, int* queue, char* scr
       __syncthreads();
     }
     if (threadIdx.x == 0) P.stats[ST_N_OPS] += (double)P.n_ops;
+    if (P.n_obs > 0) {
+      // the program's observables on this CTA (the shared memory of the
+      // update is free now): per-request completion for the serve loop
+      using EL = ExpLayout<T>;
+      static_assert(EL::smem <= Layout<T>::big, "expectation work space must fit the update's shared memory");
+      static_assert(EL::scratch <= Layout<T>::scratch, "expectation scratch must fit the update's scratch");
+      cx<T>* E = reinterpret_cast<cx<T>*>(big);
+      cx<T>* As = E + EL::e_elems;
+      cx<T>* X = EL::staged ? As + EL::a_elems : reinterpret_cast<cx<T>*>(scratch);
+      ExpTask tk;
+      tk.sites = P.sites;
+      tk.site_off = P.site_off;
+      tk.bond = P.bond;
+      tk.n = P.n;
+      tk.pad = 0;
+      for (int t = 0; t < P.n_obs; ++t) {
+        tk.codes = P.obs_codes + (size_t)t * P.n;
+        expect_sweep<T>(tk, E, As, X, P.obs_out + 2 * t);
+      }
+    }
+    if (P.done != nullptr) {
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        P.done[1] = *(volatile int*)P.err;
+        __threadfence_system();
+        *(volatile int*)P.done = 1;
+      }
+    }
     if (queue == nullptr) break;
   }
 }

@@ -121,6 +121,14 @@ struct ProgDesc {
   double cutoff;
   double* stats;            // ST_COUNT doubles
   int* err;
+  // Optional observables evaluated by the same CTA right after the ops
+  // (n_obs Pauli strings of n codes; results (re, im) per string to obs_out),
+  // then done[1] = the error word and done[0] = 1 (host-mapped memory).
+  const uint8_t* obs_codes;
+  int32_t n_obs;
+  int32_t pad2;
+  double* obs_out;
+  int* done;
 };
 
 // Measurement task descriptors (k_measure.cu).

@@ -10,6 +10,7 @@
 // run start as soon as a lane is free instead of waiting for the running
 // batch to drain.  Completed requests are finished out of order.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cstring>
 
@@ -22,6 +23,9 @@ namespace gbmps {
 // a batch fills the GPU only with ~150 circuits; more lanes let the small
 // batches that steady arrivals produce run side by side instead of queueing.
 constexpr int kServeLanes = 16;
+// Per-lane host-mapped arena for fused requests: 16 B of flags plus
+// 2 (n_terms + 1) doubles each (848 B for a 50-term Hamiltonian).
+constexpr size_t kArenaBytes = 2u << 20;
 
 static double now_ms() {
   return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
@@ -41,30 +45,73 @@ static int grow_pinned(void** p, size_t* cap, size_t need) {
   return MPS_OK;
 }
 
+static int status_of(int herr) {
+  return (herr & ERR_NAN)    ? fail(MPS_ERR_NUMERIC, "non-finite value in a two-site split")
+         : (herr & ERR_DIMS) ? fail(MPS_ERR_UNSUPPORTED, "bond dimension beyond the kernel limit")
+                             : MPS_OK;
+}
+
+// Completion bookkeeping of one request (S->mu held).
+static void complete(ServeState* S, ServeReq* r, double t) {
+  r->t_done = t;
+  r->done = true;
+  S->inflight_bytes -= r->prog->bytes;
+  S->inflight_reqs -= 1;
+}
+
+// A fused request whose flag is up (S->mu held): energy from the mapped
+// observables, status from the error word the kernel copied next to the flag.
+static void complete_fused(ServeState* S, ServeReq* r, double t) {
+  r->status = status_of(((volatile int*)r->flag)[1]);
+  r->energy = observable_value(r->prog, r->obs);
+  complete(S, r, t);
+}
+
+// Requests of a running batch whose own CTA has finished (flag in mapped
+// host memory) complete now, before the rest of the batch.
+static void reap_fused(ServeState* S, ServeBatch& B) {
+  bool any = false;
+  for (ServeReq* r : B.reqs)
+    if (r->fused && !r->done && *(volatile int*)r->flag == 1) {
+      if (!any) std::atomic_thread_fence(std::memory_order_acquire);
+      if (!any) S->mu.lock();
+      any = true;
+      complete_fused(S, r, now_ms());
+    }
+  if (any) {
+    S->mu.unlock();
+    S->cv_done.notify_all();
+  }
+}
+
 static void finish_batch(ServeState* S, ServeBatch& B) {
   const double t = now_ms();
+  std::atomic_thread_fence(std::memory_order_acquire);
   std::lock_guard<std::mutex> lk(S->mu);
   size_t ti = 0;
   size_t ri = 0;
   for (ServeReq* r : B.reqs) {
     mps_prog* p = r->prog;
     const int herr = B.h_err[ri++];
-    r->status = (herr & ERR_NAN)    ? fail(MPS_ERR_NUMERIC, "non-finite value in a two-site split")
-                : (herr & ERR_DIMS) ? fail(MPS_ERR_UNSUPPORTED, "bond dimension beyond the kernel limit")
-                                    : MPS_OK;
+    if (r->fused) {
+      if (!r->done) complete_fused(S, r, t);
+      continue;
+    }
+    r->status = status_of(herr);
     if (p->d_obs) {
       r->energy = observable_value(p, B.h_exp + 2 * ti);
       ti += (size_t)p->n_terms + 1;
     }
-    r->t_done = t;
-    r->done = true;
   }
   for (auto& bd : B.bit_dst) {
     ServeReq* r = bd.first;
     select_measured(r->prog, bd.second, r->shots, r->bits.data());
   }
-  S->inflight_bytes -= B.footprint;
-  S->inflight_reqs -= (int)B.reqs.size();
+  for (ServeReq* r : B.reqs) {
+    if (!r->fused) complete(S, r, t);
+    r->in_batch = false;
+    if (r->reaped) delete r;
+  }
   B.reqs.clear();
   B.bit_dst.clear();
   S->cv_done.notify_all();
@@ -77,16 +124,40 @@ static int launch_batch(mps_ctx* c, ServeState* S, int li, std::vector<ServeReq*
   B.footprint = 0;
   std::vector<mps_prog*> progs;
   progs.reserve(reqs.size());
+  // requests with an observable and no shots complete on their own: the
+  // update kernel evaluates the observable on the program's CTA and raises a
+  // flag in the lane's mapped arena
+  size_t aoff = 0;
   for (ServeReq* r : reqs) {
-    progs.push_back(r->prog);
-    B.footprint += r->prog->bytes;
+    mps_prog* p = r->prog;
+    progs.push_back(p);
+    B.footprint += p->bytes;
+    r->in_batch = true;
+    r->fused = false;
+    if (r->shots == 0 && p->d_obs && !prog_is_wide(p)) {
+      const size_t need = 16 + 16 * ((size_t)p->n_terms + 1);
+      if (aoff + need <= B.arena_cap) {
+        r->fused = true;
+        r->flag = reinterpret_cast<int*>(B.arena + aoff);
+        r->obs = reinterpret_cast<double*>(B.arena + aoff + 16);
+        ((volatile int*)r->flag)[0] = 0;
+        ((volatile int*)r->flag)[1] = 0;
+        p->serve_flag = r->flag;
+        p->serve_obs = r->obs;
+        aoff += need;
+      }
+    }
   }
   int rc = launch_programs(c, L, progs.data(), (int)progs.size(), false);
+  for (mps_prog* p : progs) {
+    p->serve_flag = nullptr;
+    p->serve_obs = nullptr;
+  }
   if (rc) return rc;
   B.tasks.clear();
   int prec = progs[0]->prec;
-  for (mps_prog* p : progs)
-    if (p->d_obs) observable_tasks(p, B.tasks);
+  for (ServeReq* r : reqs)
+    if (!r->fused && r->prog->d_obs) observable_tasks(r->prog, B.tasks);
   if (!B.tasks.empty()) {
     rc = grow_pinned((void**)&B.h_exp, &B.h_exp_cap, 2 * B.tasks.size() * sizeof(double));
     if (rc) return rc;
@@ -108,7 +179,7 @@ static int launch_batch(mps_ctx* c, ServeState* S, int li, std::vector<ServeReq*
     }
   }
   // error words of the batch's programs, read by finish_batch without a sync
-  rc = grow_pinned((void**)&B.h_err, &B.h_err_cap, reqs.size() * sizeof(int));
+  rc = grow_pinned((void**)&B.h_err, &B.h_err_cap, std::max<size_t>(reqs.size(), 1024) * sizeof(int));
   if (rc) return rc;
   for (size_t i = 0; i < reqs.size(); ++i) {
     cudaError_t e = cudaMemcpyAsync(B.h_err + i, reqs[i]->prog->d_err, sizeof(int), cudaMemcpyDeviceToHost, L.stream);
@@ -128,6 +199,7 @@ static void serve_loop(mps_ctx* c) {
       if (!S->lane_busy[l]) continue;
       const cudaError_t e = cudaEventQuery(S->batches[l].ev);
       if (e == cudaErrorNotReady) {
+        reap_fused(S, S->batches[l]);
         any_busy = true;
         continue;
       }
@@ -169,11 +241,11 @@ static void serve_loop(mps_ctx* c) {
         std::lock_guard<std::mutex> lk(S->mu);
         for (ServeReq* r : take) {
           r->status = rc;
-          r->t_done = now_ms();
-          r->done = true;
+          r->fused = false;
+          complete(S, r, now_ms());
+          r->in_batch = false;
+          if (r->reaped) delete r;
         }
-        for (ServeReq* r : take) S->inflight_bytes -= r->prog->bytes;
-        S->inflight_reqs -= (int)take.size();
         S->batches[free_lane].reqs.clear();
         S->cv_done.notify_all();
       } else {
@@ -256,6 +328,9 @@ int mps_serve_start(mps_ctx* c, int max_inflight) {
     e = cudaEventCreateWithFlags(&S->batches[l].ev, cudaEventDisableTiming);
     if (e != cudaSuccess) return fail(MPS_ERR_CUDA, cudaGetErrorString(e));
     S->batches[l].lane = l;
+    e = cudaHostAlloc((void**)&S->batches[l].arena, kArenaBytes, cudaHostAllocMapped);
+    if (e != cudaSuccess) return fail(MPS_ERR_OOM, cudaGetErrorString(e));
+    S->batches[l].arena_cap = kArenaBytes;
   }
   int rc = lane_init(S->wide_lane);
   if (rc) return rc;
@@ -319,7 +394,10 @@ int mps_serve_poll(mps_ctx* c, uint64_t ticket, int timeout_ms, double* energy, 
   if (bits && !r->bits.empty()) std::memcpy(bits, r->bits.data(), r->bits.size());
   if (latency_ms) *latency_ms = r->t_done - r->t_submit;
   S->all.erase(it);
-  delete r;
+  if (r->in_batch)
+    r->reaped = true;  // the running batch still holds it; finish_batch frees it
+  else
+    delete r;
   return status;
 }
 
@@ -343,6 +421,7 @@ int mps_serve_stop(mps_ctx* c) {
     if (S->batches[l].h_exp) cudaFreeHost(S->batches[l].h_exp);
     if (S->batches[l].h_bits) cudaFreeHost(S->batches[l].h_bits);
     if (S->batches[l].h_err) cudaFreeHost(S->batches[l].h_err);
+    if (S->batches[l].arena) cudaFreeHost(S->batches[l].arena);
   }
   for (auto& kv : S->all) delete kv.second;
   delete S;
