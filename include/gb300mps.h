@@ -161,7 +161,8 @@ int mps_graph_sync(mps_graph* g, double* energies);
 int mps_graph_update(mps_graph* g);
 int mps_graph_stream(mps_graph* g, void** cuda_stream);
 /* Device time of the last replay from CUDA events captured in the graph:
- * out[0] reset + fused op kernel, out[1] observables (+ copy), in ms; out[2]
+ * out[0] reset + fused op kernel (each program's observable is evaluated by
+ * its CTA after its gates), out[1] copy of the results, in ms; out[2]
  * algorithmic GEMM-class flops of the op kernel (theta merge + gate + Gram +
  * split, eigensolver excluded), out[3] eigensolver (Householder) flops, out[4]
  * bytes of the op table copied to the device by mps_graph_update, out[5]

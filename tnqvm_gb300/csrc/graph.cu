@@ -1,8 +1,9 @@
 // Captured batches: one CUDA graph per batch of programs, replayed for every
 // parameter update (the batched-VQE loop).  Body: reset every program to
 // |0...0> on the device, one persistent launch of the fused op kernel over
-// all programs, the expectation sweep of every attached observable, and the
-// copy of the raw expectation values to pinned host memory.
+// all programs (each CTA evaluates its program's attached observable right
+// after the program's gates), and the copy of the raw expectation values to
+// pinned host memory.
 #include <algorithm>
 #include <cstring>
 
@@ -112,6 +113,19 @@ int mps_graph_create(mps_ctx* c, mps_prog* const* progs, int n, mps_graph** out)
   }
   L.d_ops_cap = std::max<size_t>(g->flat.size(), 1);
   L.d_desc_cap = n;
+  g->task_first.assign(n, (size_t)-1);
+  for (int i = 0; i < n; ++i)
+    if (progs[i]->d_obs) {
+      g->task_first[i] = g->tasks.size();
+      observable_tasks(progs[i], g->tasks);
+    }
+  const int nt = (int)g->tasks.size();
+  if (nt > 0 && (cudaMalloc(&L.d_exp_out, 2 * (size_t)nt * sizeof(double)) != cudaSuccess ||
+                 cudaMallocHost(&g->h_out, 2 * (size_t)nt * sizeof(double)) != cudaSuccess)) {
+    cudaGetLastError();
+    return bail(fail(MPS_ERR_OOM, "graph expectation buffers failed"));
+  }
+  L.d_exp_out_cap = 2 * (size_t)nt;
   std::vector<ProgDesc> descs;
   for (int i : order) {
     mps_prog* p = progs[i];
@@ -129,6 +143,11 @@ int mps_graph_create(mps_ctx* c, mps_prog* const* progs, int n, mps_graph** out)
     d.cutoff = p->cutoff;
     d.stats = p->d_stats;
     d.err = p->d_err;
+    if (p->d_obs) {  // observable evaluated by the program's CTA after its gates
+      d.obs_codes = p->d_obs;
+      d.n_obs = p->n_terms + 1;
+      d.obs_out = L.d_exp_out + 2 * g->task_first[i];
+    }
     descs.push_back(d);
   }
   if (!g->flat.empty())
@@ -141,26 +160,6 @@ int mps_graph_create(mps_ctx* c, mps_prog* const* progs, int n, mps_graph** out)
     return bail(fail(MPS_ERR_OOM, "graph scratch allocation failed"));
   }
   L.op_scratch_ctas[prec] = grid;
-  g->task_first.assign(n, (size_t)-1);
-  for (int i = 0; i < n; ++i)
-    if (progs[i]->d_obs) {
-      g->task_first[i] = g->tasks.size();
-      observable_tasks(progs[i], g->tasks);
-    }
-  const int nt = (int)g->tasks.size();
-  if (nt > 0) {
-    if (cudaMalloc(&L.exp_scratch[prec], expect_scratch_bytes(prec) * (size_t)nt) != cudaSuccess ||
-        cudaMalloc(&L.d_exp_tasks, (size_t)nt * sizeof(ExpTask)) != cudaSuccess ||
-        cudaMalloc(&L.d_exp_out, 2 * (size_t)nt * sizeof(double)) != cudaSuccess ||
-        cudaMallocHost(&g->h_out, 2 * (size_t)nt * sizeof(double)) != cudaSuccess) {
-      cudaGetLastError();
-      return bail(fail(MPS_ERR_OOM, "graph expectation buffers failed"));
-    }
-    L.exp_scratch_ctas[prec] = nt;
-    L.d_exp_tasks_cap = nt;
-    L.d_exp_out_cap = 2 * (size_t)nt;
-    GCK(cudaMemcpy(L.d_exp_tasks, g->tasks.data(), (size_t)nt * sizeof(ExpTask), cudaMemcpyHostToDevice));
-  }
   cudaStream_t st = L.stream;
   for (int i = 0; i < 3; ++i)
     if (cudaEventCreate(&g->ev[i]) != cudaSuccess) return bail(fail(MPS_ERR_CUDA, "event creation failed"));
@@ -170,7 +169,6 @@ int mps_graph_create(mps_ctx* c, mps_prog* const* progs, int n, mps_graph** out)
   if (e == cudaSuccess) e = cudaMemsetAsync(L.d_queue, 0, sizeof(int), st);
   if (e == cudaSuccess) e = launch_ops(prec, L.d_desc, n, grid, n > 1 ? L.d_queue : nullptr, L.op_scratch[prec], st);
   if (e == cudaSuccess) e = cudaEventRecordWithFlags(g->ev[1], st, cudaEventRecordExternal);
-  if (e == cudaSuccess && nt > 0) e = launch_expect(prec, L.d_exp_tasks, nt, L.exp_scratch[prec], L.d_exp_out, st);
   if (e == cudaSuccess && nt > 0)
     e = cudaMemcpyAsync(g->h_out, L.d_exp_out, 2 * (size_t)nt * sizeof(double), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaEventRecordWithFlags(g->ev[2], st, cudaEventRecordExternal);
