@@ -369,8 +369,11 @@ def wide_single(args, ctx):
     terms = ["I" * i + "ZZ" + "I" * (n - i - 2) for i in range(n - 1)]
     out = {"workload": "brickwall n=48 depth=30 U3+CZ, chi<=512, cutoff 1e-10, itensor truncation, swept gate order"}
     vals = {}
+    if args.wide_autotune >= 0:
+        M.autotune_set_mode(args.wide_autotune)
     for prec in ([M.PREC_FP32, M.PREC_FP64] if args.wide_ref else [M.PREC_FP32]):
         tc0, _ = ctx.gemm_counts()
+        tu0 = ctx.autotune_tunings()
         t0 = time.perf_counter()
         p = M.Program(ctx, n, chi, cut, M.TRUNC_ITENSOR, prec, M.FLAG_SWEEP)
         p.run(circ)
@@ -384,8 +387,13 @@ def wide_single(args, ctx):
         vals[key] = v
         out[key] = {"seconds": t1 - t0, "circuits_per_s": 1.0 / (t1 - t0), "splits": st["gate2"], "ops": st["ops"],
                     "max_bond": max(p.bond_dims()), "truncation_fidelity": float(st["fidelity"]),
-                    "tensor_core_gemms": tc1 - tc0}
+                    "tensor_core_gemms": tc1 - tc0,
+                    "gemm_buckets_tuned": ctx.autotune_tunings() - tu0}
         p.close()
+    table = M.autotune_table()
+    out["gemm_autotune"] = {"mode": M.autotune_mode(), "buckets": len(table),
+                            "kernels": {name: sum(1 for r in table if r["kernel"] == k)
+                                        for k, name in enumerate(M.GEMM_KERNEL_NAMES)}}
     if "c128" in vals:
         d = np.abs(vals["c64"] - vals["c128"])
         out["err_c64_vs_c128"] = {"max_abs_dZZ": float(d.max()), "median_abs_dZZ": float(np.median(d))}
@@ -491,6 +499,8 @@ def main():
     ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--wide", type=int, default=1, help="time the 48-qubit chi=512 circuit (1/0)")
     ap.add_argument("--wide-ref", action="store_true", help="also run it in complex128 and report the error")
+    ap.add_argument("--wide-autotune", type=int, default=-1,
+                    help="GEMM autotuner mode for the wide circuit (0 static, 1 tune, 2 table; -1 library default)")
     ap.add_argument("--serve-mix", type=int, default=0, help="requests of the mixed-cap serving stream (0: off)")
     ap.add_argument("--serve-mix-rate", type=float, default=100.0)
     ap.add_argument("--qmax", type=int, default=32, help="largest qubit count (small profiling cases)")

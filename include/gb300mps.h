@@ -237,6 +237,48 @@ int mps_diag_cgemm(mps_ctx* ctx, int M, int N, int K, const double* a, const dou
                    double* c_simt);
 int mps_diag_gemm_counts(mps_ctx* ctx, int* tensor_core, int* cuda_core);
 
+/* GEMM autotuner of the wide path; no counterpart in the reference (its
+ * contractions go through ExaTN or ITensor/LAPACK, which pick their own
+ * kernels).  Every complex product of the wide path can run on one of these
+ * kernels: */
+#define MPS_GEMM_SIMT_64x64 0 /* CUDA cores, 64 x 64 complex outputs per CTA */
+#define MPS_GEMM_SIMT_32x32 1 /* CUDA cores, 32 x 32 */
+#define MPS_GEMM_SIMT_16x64 2 /* CUDA cores, 16 rows x 64 columns (short, wide outputs) */
+#define MPS_GEMM_SIMT_64x16 3 /* CUDA cores, 64 rows x 16 columns (tall, thin outputs) */
+#define MPS_GEMM_TC 4         /* complex64 only: tcgen05 3xTF32, 128 x 64 complex per CTA */
+#define MPS_GEMM_KERNELS 5
+/* Modes: 0 a static rule (tensor cores for complex64 products of at least
+ * ~2M complex MACs, else 64 x 64 tiles); 1 tune: the first product of each
+ * new bucket (device, precision, ceil(log2) of M, N and K, and which index
+ * of A, B and C is unit-stride) times every kernel that can take it on the
+ * caller's stream, writing a scratch output (the inputs are only read), then
+ * uses the fastest unless the static rule is within 5 %; 2 use tuned or
+ * loaded entries only.  The CUDA-core tiles give bit-identical results; the
+ * tensor-core kernel differs from them by FP32 rounding (~1e-6 relative).
+ * Tuning synchronises the stream and allocates a 64 MiB scratch buffer per
+ * workspace once, so it is skipped inside a stream capture.  The initial
+ * mode comes from the environment variable GB300MPS_AUTOTUNE (default 0).
+ * The table is process-wide. */
+#define MPS_AUTOTUNE_COLS 9
+int mps_autotune_set_mode(int mode);
+int mps_autotune_get_mode(int* mode);
+/* Rows of MPS_AUTOTUNE_COLS ints: device, precision, ceil(log2) of M, N and K,
+ * layout bits (1 A's rows unit-stride, 2 B's columns, 4 C's rows), chosen
+ * kernel, its time per launch in ns, the static rule's time in ns.  Writes at
+ * most cap rows; *n_entries receives the table size. */
+int mps_autotune_table(int* out, int cap, int* n_entries);
+/* Text cache of the table (one line per bucket), so a later process can
+ * start from it in mode 2 without trial launches. */
+int mps_autotune_save(const char* path);
+int mps_autotune_load(const char* path);
+int mps_autotune_clear(void);
+/* Buckets tuned by this context's wide workspaces so far. */
+int mps_autotune_tunings(mps_ctx* ctx, int* out);
+/* One product C = A B (host arrays of interleaved doubles, row-major) on a
+ * chosen kernel; flags bit 0/1/2 store A/B/C column-major on the device. */
+int mps_diag_cgemm_kind(mps_ctx* ctx, int precision, int kernel, int flags, int M, int N, int K, const double* a,
+                        const double* b, double* out);
+
 /* Footprint used by admission: sum over sites of chi_l * 2 * chi_r * bytes. */
 size_t mps_footprint_bytes(int n_qubits, int chi_max, int precision);
 

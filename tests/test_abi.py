@@ -61,3 +61,43 @@ def test_no_device_is_an_error_not_a_crash():
     with pytest.raises(M.MpsError) as e:
         M.Context(0)
     assert e.value.code == M.ERR_CUDA
+
+
+def test_autotune_host_calls(tmp_path):
+    """The GEMM autotuner's mode, table and text cache work without a GPU:
+    mode validation, a save/load round trip of a hand-written entry, and a
+    malformed cache rejected without touching the table."""
+    from tnqvm_gb300 import mps as M
+    old = M.autotune_mode()
+    try:
+        with pytest.raises(M.MpsError) as e:
+            M.autotune_set_mode(3)
+        assert e.value.code == M.ERR_ARG
+        M.autotune_set_mode(2)
+        assert M.autotune_mode() == 2
+        M.autotune_clear()
+        assert M.autotune_table() == []
+        # bucket: device 0, complex64 (1), M in (128, 256], N in (256, 512],
+        # K in (512, 1024], A rows and B columns unit-stride (layout 3)
+        key = (0 << 20) | (1 << 19) | (8 << 15) | (9 << 11) | (10 << 7) | 3
+        src = tmp_path / "tune.txt"
+        src.write_text("# comment\n%d 1 0 900.0 450.5 700.0 800.0 0.0\n" % key)
+        M.autotune_load(str(src))
+        rows = M.autotune_table()
+        assert rows == [dict(device=0, precision=1, lg_m=8, lg_n=9, lg_k=10, layout=3, kernel=1, ns=450,
+                             static_ns=900)]
+        out = tmp_path / "saved.txt"
+        M.autotune_save(str(out))
+        M.autotune_clear()
+        M.autotune_load(str(out))
+        assert M.autotune_table() == rows
+        bad = tmp_path / "bad.txt"
+        bad.write_text("%d 9 0 1 2 3 4 5\n" % key)
+        with pytest.raises(M.MpsError):
+            M.autotune_load(str(bad))
+        assert M.autotune_table() == rows
+        with pytest.raises(M.MpsError):
+            M.autotune_load(str(tmp_path / "missing.txt"))
+    finally:
+        M.autotune_clear()
+        M.autotune_set_mode(old)

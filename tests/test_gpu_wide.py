@@ -92,14 +92,19 @@ def test_wide_exact_fp32(ctx, mode):
     n = 14
     circ = circuits.brickwall(n, 14, seed=21)
     psi = dense.run(n, circ)
-    t0, _ = ctx.gemm_counts()
-    with run(ctx, n, circ, 128, 1e-14, mode, M.PREC_FP32) as p:
-        amp = p.amplitudes()
-        assert np.max(np.abs(amp - psi)) < 1e-4
-        zs = p.expect_pauli(["I" * q + "Z" + "I" * (n - q - 1) for q in range(n)])
-        for q in range(n):
-            assert abs(zs[q].real - dense.expect_z_parity(psi, [q])) < 2e-5
-    t1, _ = ctx.gemm_counts()
+    old = M.autotune_mode()
+    M.autotune_set_mode(0)  # the static rule puts the large products on tensor cores
+    try:
+        t0, _ = ctx.gemm_counts()
+        with run(ctx, n, circ, 128, 1e-14, mode, M.PREC_FP32) as p:
+            amp = p.amplitudes()
+            assert np.max(np.abs(amp - psi)) < 1e-4
+            zs = p.expect_pauli(["I" * q + "Z" + "I" * (n - q - 1) for q in range(n)])
+            for q in range(n):
+                assert abs(zs[q].real - dense.expect_z_parity(psi, [q])) < 2e-5
+        t1, _ = ctx.gemm_counts()
+    finally:
+        M.autotune_set_mode(old)
     assert t1 > t0  # the tensor-core kernel ran
 
 

@@ -15,6 +15,7 @@
 #include "../../include/gb300mps.h"
 #include "engine_internal.hpp"
 #include "gates.hpp"
+#include "wide.hpp"
 
 namespace gbmps {
 
@@ -1086,6 +1087,64 @@ int mps_diag_cgemm(mps_ctx* c, int M, int N, int K, const double* a, const doubl
 int mps_diag_gemm_counts(mps_ctx* c, int* tensor_core, int* cuda_core) {
   if (!c || !tensor_core || !cuda_core) return fail(MPS_ERR_ARG, "NULL argument");
   return wide_gemm_counts(c, tensor_core, cuda_core);
+}
+
+int mps_diag_cgemm_kind(mps_ctx* c, int precision, int kernel, int flags, int M, int N, int K, const double* a,
+                        const double* b, double* out) {
+  if (!c || !a || !b || !out || M < 1 || N < 1 || K < 1 || M > 4096 || N > 4096 || K > 4096 || kernel < 0 ||
+      kernel >= MPS_GEMM_KERNELS || (precision != MPS_PREC_FP64 && precision != MPS_PREC_FP32) || flags < 0 ||
+      flags > 7)
+    return fail(MPS_ERR_ARG, "bad argument");
+  if (precision == MPS_PREC_FP64 && kernel == MPS_GEMM_TC)
+    return fail(MPS_ERR_ARG, "the tensor-core GEMM takes complex64 only");
+  std::lock_guard<std::mutex> lk(c->mu);
+  CK(cudaSetDevice(c->device));
+  return wide_diag_cgemm_kind(c, precision, kernel, flags, M, N, K, a, b, out);
+}
+
+int mps_autotune_set_mode(int mode) {
+  if (mode < 0 || mode > 2) return fail(MPS_ERR_ARG, "autotune mode must be 0, 1 or 2");
+  gemm_tune_set_mode(mode);
+  return MPS_OK;
+}
+
+int mps_autotune_get_mode(int* mode) {
+  if (!mode) return fail(MPS_ERR_ARG, "NULL argument");
+  *mode = gemm_tune_mode();
+  return MPS_OK;
+}
+
+int mps_autotune_table(int* out, int cap, int* n_entries) {
+  if (!n_entries || cap < 0 || (cap > 0 && !out)) return fail(MPS_ERR_ARG, "bad argument");
+  static_assert(MPS_AUTOTUNE_COLS == kTuneCols, "autotune table row width");
+  *n_entries = gemm_tune_table(out, cap);
+  return MPS_OK;
+}
+
+int mps_autotune_save(const char* path) {
+  if (!path) return fail(MPS_ERR_ARG, "NULL argument");
+  if (gemm_tune_save(path)) return fail(MPS_ERR_ARG, std::string("cannot write ") + path);
+  return MPS_OK;
+}
+
+int mps_autotune_load(const char* path) {
+  if (!path) return fail(MPS_ERR_ARG, "NULL argument");
+  const int rc = gemm_tune_load(path);
+  if (rc == 1) return fail(MPS_ERR_ARG, std::string("cannot read ") + path);
+  if (rc) return fail(MPS_ERR_ARG, std::string("malformed tuning file ") + path);
+  return MPS_OK;
+}
+
+int mps_autotune_clear(void) {
+  gemm_tune_clear();
+  return MPS_OK;
+}
+
+int mps_autotune_tunings(mps_ctx* c, int* out) {
+  if (!c || !out) return fail(MPS_ERR_ARG, "NULL argument");
+  std::lock_guard<std::mutex> lk(c->mu);
+  *out = wide_gemm_tunings(c);
+  return MPS_OK;
 }
 
 int mps_bond_dims(mps_prog* p, int* out) {

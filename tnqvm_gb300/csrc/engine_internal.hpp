@@ -194,5 +194,8 @@ int wide_amp_one(::mps_prog* p, const int* bits, double* out);
 int wide_gemm_counts(mps_ctx* c, int* tc, int* simt);
 int wide_diag_cgemm(mps_ctx* c, int M, int N, int K, const double* a, const double* b, double* out_tc,
                     double* out_simt);
+int wide_diag_cgemm_kind(mps_ctx* c, int prec, int kind, int flags, int M, int N, int K, const double* a,
+                         const double* b, double* out);
+int wide_gemm_tunings(mps_ctx* c);
 void wide_free(mps_ctx* c);
 }  // namespace gbmps

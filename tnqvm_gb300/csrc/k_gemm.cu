@@ -24,6 +24,9 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
+#include <cstdio>
+#include <cstdlib>
+#include <map>
 #include <mutex>
 
 #include "wide.hpp"
@@ -31,7 +34,10 @@
 namespace gbmps {
 
 // ------------------------------------------------------------ CUDA cores
-constexpr int kSB = 64;   // 64 x 64 complex outputs per CTA
+// Output tiles of BM x BN complex entries per 256-thread CTA (16 x 16
+// threads, each holding (BM/16) x (BN/16) accumulators).  Every output sums
+// its K terms in the same order whatever the tile, so the tile shapes give
+// bit-identical results; the autotuner below picks among them by speed.
 constexpr int kSK = 16;
 
 template <typename T>
@@ -42,36 +48,39 @@ __device__ __forceinline__ cx<T> vload(const CMat<T>& v, int i, int j) {
   return z;
 }
 
-template <typename T>
+template <typename T, int BM, int BN>
 __global__ void __launch_bounds__(256) k_cgemm_simt(CMat<T> A, CMat<T> B, CMatOut<T> C, T alpha, T beta) {
-  __shared__ cx<T> As[kSK][kSB + 1];
-  __shared__ cx<T> Bs[kSK][kSB + 1];
-  const int i0 = blockIdx.y * kSB, j0 = blockIdx.x * kSB;
+  constexpr int RM = BM / 16, RN = BN / 16;
+  __shared__ cx<T> As[kSK][BM + 1];
+  __shared__ cx<T> Bs[kSK][BN + 1];
+  const int i0 = blockIdx.y * BM, j0 = blockIdx.x * BN;
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
   const int K = A.cols;
-  cx<T> acc[4][4];
+  cx<T> acc[RM][RN];
 #pragma unroll
-  for (int a = 0; a < 4; ++a)
+  for (int a = 0; a < RM; ++a)
 #pragma unroll
-    for (int b = 0; b < 4; ++b) acc[a][b] = mk<T>(T(0), T(0));
+    for (int b = 0; b < RN; ++b) acc[a][b] = mk<T>(T(0), T(0));
   // lanes walk the unit-stride index of each view (coalesced loads)
   const bool a_rows_fast = A.rs == 1 && A.cs != 1;
   const bool b_cols_fast = !(B.rs == 1 && B.cs != 1);
   for (int k0 = 0; k0 < K; k0 += kSK) {
-    for (int t = threadIdx.x; t < kSB * kSK; t += 256) {
+    for (int t = threadIdx.x; t < BM * kSK; t += 256) {
       int ii, kk;
       if (a_rows_fast) {
-        ii = t % kSB;
-        kk = t / kSB;
+        ii = t % BM;
+        kk = t / BM;
       } else {
         kk = t % kSK;
         ii = t / kSK;
       }
       As[kk][ii] = vload(A, i0 + ii, k0 + kk);
+    }
+    for (int t = threadIdx.x; t < BN * kSK; t += 256) {
       int jj, k2;
       if (b_cols_fast) {
-        jj = t % kSB;
-        k2 = t / kSB;
+        jj = t % BN;
+        k2 = t / BN;
       } else {
         k2 = t % kSK;
         jj = t / kSK;
@@ -81,24 +90,24 @@ __global__ void __launch_bounds__(256) k_cgemm_simt(CMat<T> A, CMat<T> B, CMatOu
     __syncthreads();
 #pragma unroll 4
     for (int kk = 0; kk < kSK; ++kk) {
-      cx<T> a[4], b[4];
+      cx<T> a[RM], b[RN];
 #pragma unroll
-      for (int r = 0; r < 4; ++r) a[r] = As[kk][ty + 16 * r];
+      for (int r = 0; r < RM; ++r) a[r] = As[kk][ty + 16 * r];
 #pragma unroll
-      for (int c = 0; c < 4; ++c) b[c] = Bs[kk][tx + 16 * c];
+      for (int c = 0; c < RN; ++c) b[c] = Bs[kk][tx + 16 * c];
 #pragma unroll
-      for (int r = 0; r < 4; ++r)
+      for (int r = 0; r < RM; ++r)
 #pragma unroll
-        for (int c = 0; c < 4; ++c) fma_c(acc[r][c], a[r], b[c]);
+        for (int c = 0; c < RN; ++c) fma_c(acc[r][c], a[r], b[c]);
     }
     __syncthreads();
   }
 #pragma unroll
-  for (int r = 0; r < 4; ++r) {
+  for (int r = 0; r < RM; ++r) {
     const int i = i0 + ty + 16 * r;
     if (i >= C.rows) continue;
 #pragma unroll
-    for (int c = 0; c < 4; ++c) {
+    for (int c = 0; c < RN; ++c) {
       const int j = j0 + tx + 16 * c;
       if (j >= C.cols) continue;
       cx<T>* dst = C.p + (int64_t)i * C.rs + (int64_t)j * C.cs;
@@ -109,13 +118,28 @@ __global__ void __launch_bounds__(256) k_cgemm_simt(CMat<T> A, CMat<T> B, CMatOu
   }
 }
 
+template <typename T, int BM, int BN>
+static cudaError_t simt_tile(const CMat<T>& A, const CMat<T>& B, const CMatOut<T>& C, T alpha, T beta,
+                             cudaStream_t st) {
+  dim3 grid((C.cols + BN - 1) / BN, (C.rows + BM - 1) / BM);
+  k_cgemm_simt<T, BM, BN><<<grid, 256, 0, st>>>(A, B, C, alpha, beta);
+  return cudaGetLastError();
+}
+
 template <typename T>
 static cudaError_t simt_launch(const CMat<T>& A, const CMat<T>& B, const CMatOut<T>& C, T alpha, T beta,
-                               cudaStream_t st) {
+                               cudaStream_t st, int kind = GEMM_SIMT_64x64) {
   if (C.rows <= 0 || C.cols <= 0) return cudaSuccess;
-  dim3 grid((C.cols + kSB - 1) / kSB, (C.rows + kSB - 1) / kSB);
-  k_cgemm_simt<T><<<grid, 256, 0, st>>>(A, B, C, alpha, beta);
-  return cudaGetLastError();
+  switch (kind) {
+    case GEMM_SIMT_32x32:
+      return simt_tile<T, 32, 32>(A, B, C, alpha, beta, st);
+    case GEMM_SIMT_16x64:
+      return simt_tile<T, 16, 64>(A, B, C, alpha, beta, st);
+    case GEMM_SIMT_64x16:
+      return simt_tile<T, 64, 16>(A, B, C, alpha, beta, st);
+    default:
+      return simt_tile<T, 64, 64>(A, B, C, alpha, beta, st);
+  }
 }
 
 // ------------------------------------------------------------ tcgen05 path
@@ -420,7 +444,37 @@ void gemm_ws_free(GemmWs& ws) {
   if (ws.b_hi) cudaFree(ws.b_hi);
   if (ws.b_lo) cudaFree(ws.b_lo);
   if (ws.d_err) cudaFree(ws.d_err);
+  if (ws.tune_c) cudaFree(ws.tune_c);
+  for (cudaEvent_t e : ws.tune_ev)
+    if (e) cudaEventDestroy(e);
   ws = GemmWs();
+}
+
+// The tensor-core kernel takes products with N, K >= 16 whose padded
+// operands fit the workspace.
+static bool tc_eligible(int M, int N, int K, const GemmWs& ws) {
+  if (N < 16 || K < 16 || !get_encode()) return false;
+  const size_t mp = (size_t)(M + tc::BM - 1) / tc::BM * tc::BM;
+  const size_t np = (size_t)(2 * N + tc::BN - 1) / tc::BN * tc::BN;
+  const size_t kp = (size_t)(2 * K + tc::KP_ALIGN - 1) / tc::KP_ALIGN * tc::KP_ALIGN;
+  return mp * kp <= ws.a_elems && np * kp <= ws.b_elems;
+}
+
+static cudaError_t tc_launch(const CMat<float>& A, const CMat<float>& B, const CMatOut<float>& C, float alpha,
+                             float beta, GemmWs& ws, cudaStream_t st) {
+  const int M = C.rows, N = C.cols, K = A.cols;
+  const int mp = (M + tc::BM - 1) / tc::BM * tc::BM;
+  const int np = (2 * N + tc::BN - 1) / tc::BN * tc::BN;
+  const int kp = (2 * K + tc::KP_ALIGN - 1) / tc::KP_ALIGN * tc::KP_ALIGN;
+  k_pack<false><<<dim3(kp / 64, mp / 32), 256, 0, st>>>(A, ws.a_hi, ws.a_lo, kp);
+  k_pack<true><<<dim3(kp / 64, np / 64), 256, 0, st>>>(B, ws.b_hi, ws.b_lo, kp);
+  CUtensorMap ma, mal, mb, mbl;
+  if (!make_map(&ma, ws.a_hi, mp, kp) || !make_map(&mal, ws.a_lo, mp, kp) || !make_map(&mb, ws.b_hi, np, kp) ||
+      !make_map(&mbl, ws.b_lo, np, kp))
+    return cudaErrorInvalidValue;
+  k_cgemm_tc<<<dim3(np / tc::BN, mp / tc::BM), 128, tc::SMEM, st>>>(ma, mal, mb, mbl, kp / tc::BK, C, alpha, beta,
+                                                                    ws.d_err);
+  return cudaGetLastError();
 }
 
 cudaError_t cgemm_simt(const CMat<float>& A, const CMat<float>& B, const CMatOut<float>& C, float alpha, float beta,
@@ -428,39 +482,265 @@ cudaError_t cgemm_simt(const CMat<float>& A, const CMat<float>& B, const CMatOut
   return simt_launch<float>(A, B, C, alpha, beta, st);
 }
 
+cudaError_t cgemm_kind(int kind, const CMat<float>& A, const CMat<float>& B, const CMatOut<float>& C, float alpha,
+                       float beta, GemmWs& ws, cudaStream_t st) {
+  if (C.rows <= 0 || C.cols <= 0) return cudaSuccess;
+  if (kind == GEMM_TC) {
+    if (!tc_eligible(C.rows, C.cols, A.cols, ws)) return cudaErrorInvalidValue;
+    return tc_launch(A, B, C, alpha, beta, ws, st);
+  }
+  if (kind < 0 || kind >= GEMM_TC) return cudaErrorInvalidValue;
+  return simt_launch<float>(A, B, C, alpha, beta, st, kind);
+}
+
+cudaError_t cgemm_kind(int kind, const CMat<double>& A, const CMat<double>& B, const CMatOut<double>& C,
+                       double alpha, double beta, GemmWs&, cudaStream_t st) {
+  if (kind < 0 || kind >= GEMM_TC) return cudaErrorInvalidValue;
+  return simt_launch<double>(A, B, C, alpha, beta, st, kind);
+}
+
+// ------------------------------------------------------------ autotuner
+namespace {
+
+struct TuneEntry {
+  int kind;                   // chosen kernel
+  float ns[GEMM_KINDS];       // measured time per launch (0: not eligible)
+  int static_kind;            // kernel of the static rule for this bucket
+};
+
+std::mutex g_tune_mu;
+std::map<uint32_t, TuneEntry> g_tune;
+int g_tune_mode = -1;  // -1: not read from the environment yet
+
+constexpr size_t kTuneMaxBytes = size_t(64) << 20;  // largest trial output (64 MiB)
+constexpr int kTuneReps = 3;                         // timed launches per kernel after one warm-up
+constexpr float kTuneMargin = 0.95f;                 // a kernel must beat the static rule by 5 %
+
+int lg2(int x) {
+  int l = 0;
+  while ((1 << l) < x && l < 15) ++l;
+  return l;
+}
+
+// Which index of each view is unit-stride: bit 0 A's rows, bit 1 B's
+// columns, bit 2 C's rows.
+template <typename T>
+int layout_bits(const CMat<T>& A, const CMat<T>& B, const CMatOut<T>& C) {
+  return (A.rs == 1 && A.cs != 1 ? 1 : 0) | (!(B.rs == 1 && B.cs != 1) ? 2 : 0) | (C.rs == 1 && C.cs != 1 ? 4 : 0);
+}
+
+uint32_t tune_key(int dev, int prec, int M, int N, int K, int layout) {
+  return ((uint32_t)(dev & 63) << 20) | ((uint32_t)(prec & 1) << 19) | ((uint32_t)lg2(M) << 15) |
+         ((uint32_t)lg2(N) << 11) | ((uint32_t)lg2(K) << 7) | (uint32_t)(layout & 7);
+}
+
+int mode_now() {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  if (g_tune_mode < 0) {
+    const char* e = getenv("GB300MPS_AUTOTUNE");
+    g_tune_mode = (e && *e) ? atoi(e) : 0;
+    if (g_tune_mode < 0 || g_tune_mode > 2) g_tune_mode = 0;
+  }
+  return g_tune_mode;
+}
+
+template <typename T>
+int static_kind(int M, int N, int K, const GemmWs& ws) {
+  if (sizeof(T) == 8) return GEMM_SIMT_64x64;  // complex128: CUDA cores only
+  // small products (under ~2M complex MACs, or too thin to fill a tile
+  // pair) stay on the CUDA cores; the rest are padded to 128 x 128 tiles
+  if ((double)M * N * K < 2097152.0 || !tc_eligible(M, N, K, ws)) return GEMM_SIMT_64x64;
+  return GEMM_TC;
+}
+
+// Time every eligible kernel on this product, writing a scratch output of
+// C's shape and layout (alpha 1, beta 0), and record the fastest.  Returns
+// the kernel to use; on a trial failure returns -1 with the error in *err.
+template <typename T>
+int tune_bucket(uint32_t key, const CMat<T>& A, const CMat<T>& B, const CMatOut<T>& C, GemmWs& ws, int skind,
+                cudaStream_t st, cudaError_t* err) {
+  *err = cudaSuccess;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(st, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone) {
+    cudaGetLastError();
+    return skind;  // no trial launches or allocation inside a capture
+  }
+  const int M = C.rows, N = C.cols;
+  const size_t bytes = (size_t)M * N * sizeof(cx<T>);
+  if (bytes > kTuneMaxBytes) return skind;
+  if (ws.tune_c_bytes < bytes) {
+    if (ws.tune_c) cudaFree(ws.tune_c);
+    ws.tune_c = nullptr;
+    ws.tune_c_bytes = 0;
+    if (cudaMalloc(&ws.tune_c, kTuneMaxBytes) != cudaSuccess) {
+      cudaGetLastError();
+      ws.tune_c = nullptr;
+      return skind;
+    }
+    ws.tune_c_bytes = kTuneMaxBytes;
+  }
+  for (cudaEvent_t& e : ws.tune_ev)
+    if (!e && cudaEventCreate(&e) != cudaSuccess) {
+      cudaGetLastError();
+      e = nullptr;
+      return skind;
+    }
+  // the trial output keeps C's layout (row- or column-major)
+  const CMatOut<T> Ct = (C.rs == 1 && C.cs != 1) ? cout_<T>(ws.tune_c, M, N, 1, M) : cout_<T>(ws.tune_c, M, N, N, 1);
+  TuneEntry en;
+  en.static_kind = skind;
+  for (float& t : en.ns) t = 0.0f;
+  for (int kind = 0; kind < GEMM_KINDS; ++kind) {
+    if (kind == GEMM_TC && (sizeof(T) == 8 || !tc_eligible(M, N, A.cols, ws))) continue;
+    cudaError_t e = cgemm_kind(kind, A, B, Ct, T(1), T(0), ws, st);
+    if (e == cudaSuccess) e = cudaEventRecord(ws.tune_ev[0], st);
+    for (int r = 0; r < kTuneReps && e == cudaSuccess; ++r) e = cgemm_kind(kind, A, B, Ct, T(1), T(0), ws, st);
+    if (e == cudaSuccess) e = cudaEventRecord(ws.tune_ev[1], st);
+    if (e == cudaSuccess) e = cudaEventSynchronize(ws.tune_ev[1]);
+    float ms = 0.0f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, ws.tune_ev[0], ws.tune_ev[1]);
+    if (e != cudaSuccess) {
+      *err = e;
+      return -1;
+    }
+    en.ns[kind] = ms * 1e6f / kTuneReps;
+  }
+  // the static rule unless another kernel beats it by the margin; then the fastest
+  int best = skind;
+  float best_ns = en.ns[skind];
+  for (int kind = 0; kind < GEMM_KINDS; ++kind)
+    if (en.ns[kind] > 0.0f && en.ns[kind] < en.ns[skind] * kTuneMargin && en.ns[kind] < best_ns) {
+      best = kind;
+      best_ns = en.ns[kind];
+    }
+  en.kind = best;
+  ++ws.tunings;
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune[key] = en;
+  return best;
+}
+
+template <typename T>
+cudaError_t cgemm_tuned(const CMat<T>& A, const CMat<T>& B, const CMatOut<T>& C, T alpha, T beta, GemmWs& ws,
+                        cudaStream_t st) {
+  const int M = C.rows, N = C.cols, K = A.cols;
+  if (M <= 0 || N <= 0) return cudaSuccess;
+  const int skind = static_kind<T>(M, N, K, ws);
+  int kind = skind;
+  const int mode = mode_now();
+  if (mode != 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    // precision as in the C ABI: 0 complex128, 1 complex64
+    const uint32_t key = tune_key(dev, sizeof(T) == 8 ? 0 : 1, M, N, K, layout_bits(A, B, C));
+    bool found = false;
+    {
+      std::lock_guard<std::mutex> lk(g_tune_mu);
+      auto it = g_tune.find(key);
+      if (it != g_tune.end()) {
+        kind = it->second.kind;
+        found = true;
+      }
+    }
+    if (!found && mode == 1) {
+      cudaError_t e;
+      kind = tune_bucket<T>(key, A, B, C, ws, skind, st, &e);
+      if (kind < 0) return e;
+    }
+    // an entry tuned on a larger workspace may name a kernel this product cannot take here
+    if (kind == GEMM_TC && (sizeof(T) == 8 || !tc_eligible(M, N, K, ws))) kind = skind;
+  }
+  if (kind == GEMM_TC)
+    ++ws.tc_launches;
+  else
+    ++ws.simt_launches;
+  return cgemm_kind(kind, A, B, C, alpha, beta, ws, st);
+}
+
+}  // namespace
+
 cudaError_t cgemm(const CMat<double>& A, const CMat<double>& B, const CMatOut<double>& C, double alpha, double beta,
                   GemmWs& ws, cudaStream_t st) {
-  ++ws.simt_launches;
-  return simt_launch<double>(A, B, C, alpha, beta, st);
+  return cgemm_tuned<double>(A, B, C, alpha, beta, ws, st);
 }
 
 cudaError_t cgemm(const CMat<float>& A, const CMat<float>& B, const CMatOut<float>& C, float alpha, float beta,
                   GemmWs& ws, cudaStream_t st) {
-  const int M = C.rows, N = C.cols, K = A.cols;
-  if (M <= 0 || N <= 0) return cudaSuccess;
-  // small products (under ~2M complex MACs, or too thin to fill a tile
-  // pair) stay on the CUDA cores; the rest are padded to 128 x 128 tiles
-  if ((double)M * N * K < 2097152.0 || N < 16 || K < 16 || !get_encode()) {
-    ++ws.simt_launches;
-    return simt_launch<float>(A, B, C, alpha, beta, st);
+  return cgemm_tuned<float>(A, B, C, alpha, beta, ws, st);
+}
+
+void gemm_tune_set_mode(int mode) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune_mode = (mode < 0 || mode > 2) ? 0 : mode;
+}
+
+int gemm_tune_mode() { return mode_now(); }
+
+void gemm_tune_clear() {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune.clear();
+}
+
+static void entry_row(uint32_t key, const TuneEntry& en, int* row) {
+  row[0] = (int)((key >> 20) & 63);
+  row[1] = (int)((key >> 19) & 1);
+  row[2] = (int)((key >> 15) & 15);
+  row[3] = (int)((key >> 11) & 15);
+  row[4] = (int)((key >> 7) & 15);
+  row[5] = (int)(key & 7);
+  row[6] = en.kind;
+  row[7] = (int)en.ns[en.kind];
+  row[8] = (int)en.ns[en.static_kind];
+}
+
+int gemm_tune_table(int* out, int cap) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  int n = 0;
+  for (const auto& kv : g_tune) {
+    if (out && n < cap) entry_row(kv.first, kv.second, out + (size_t)n * kTuneCols);
+    ++n;
   }
-  const int mp = (M + tc::BM - 1) / tc::BM * tc::BM;
-  const int np = (2 * N + tc::BN - 1) / tc::BN * tc::BN;
-  const int kp = (2 * K + tc::KP_ALIGN - 1) / tc::KP_ALIGN * tc::KP_ALIGN;
-  if ((size_t)mp * kp > ws.a_elems || (size_t)np * kp > ws.b_elems) {
-    ++ws.simt_launches;
-    return simt_launch<float>(A, B, C, alpha, beta, st);
+  return n;
+}
+
+// Text cache: one line per bucket, "key kind static_kind ns_0 .. ns_4".
+int gemm_tune_save(const char* path) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  FILE* f = fopen(path, "w");
+  if (!f) return 1;
+  fprintf(f, "# gb300mps gemm tuning v1: key kind static_kind ns[%d]\n", (int)GEMM_KINDS);
+  for (const auto& kv : g_tune) {
+    fprintf(f, "%u %d %d", kv.first, kv.second.kind, kv.second.static_kind);
+    for (float t : kv.second.ns) fprintf(f, " %.1f", t);
+    fprintf(f, "\n");
   }
-  k_pack<false><<<dim3(kp / 64, mp / 32), 256, 0, st>>>(A, ws.a_hi, ws.a_lo, kp);
-  k_pack<true><<<dim3(kp / 64, np / 64), 256, 0, st>>>(B, ws.b_hi, ws.b_lo, kp);
-  CUtensorMap ma, mal, mb, mbl;
-  if (!make_map(&ma, ws.a_hi, mp, kp) || !make_map(&mal, ws.a_lo, mp, kp) || !make_map(&mb, ws.b_hi, np, kp) ||
-      !make_map(&mbl, ws.b_lo, np, kp))
-    return cudaErrorInvalidValue;
-  ++ws.tc_launches;
-  k_cgemm_tc<<<dim3(np / tc::BN, mp / tc::BM), 128, tc::SMEM, st>>>(ma, mal, mb, mbl, kp / tc::BK, C, alpha, beta,
-                                                                    ws.d_err);
-  return cudaGetLastError();
+  return fclose(f) == 0 ? 0 : 1;
+}
+
+int gemm_tune_load(const char* path) {
+  FILE* f = fopen(path, "r");
+  if (!f) return 1;
+  char line[512];
+  std::map<uint32_t, TuneEntry> got;
+  bool bad = false;
+  while (fgets(line, sizeof line, f)) {
+    if (line[0] == '#' || line[0] == '\n') continue;
+    unsigned key = 0;
+    TuneEntry en;
+    int n = sscanf(line, "%u %d %d %f %f %f %f %f", &key, &en.kind, &en.static_kind, &en.ns[0], &en.ns[1], &en.ns[2],
+                   &en.ns[3], &en.ns[4]);
+    if (n != 3 + GEMM_KINDS || en.kind < 0 || en.kind >= GEMM_KINDS || en.static_kind < 0 ||
+        en.static_kind >= GEMM_KINDS || (key >> 26) != 0) {
+      bad = true;
+      break;
+    }
+    got[(uint32_t)key] = en;
+  }
+  fclose(f);
+  if (bad) return 2;
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  for (const auto& kv : got) g_tune[kv.first] = kv.second;
+  return 0;
 }
 
 }  // namespace gbmps

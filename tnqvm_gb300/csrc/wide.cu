@@ -905,10 +905,19 @@ int wide_diag_cgemm(mps_ctx* c, int M, int N, int K, const double* a, const doub
   WCK(cudaMemcpyAsync(da, ha.data(), ha.size() * 8, cudaMemcpyHostToDevice, st));
   WCK(cudaMemcpyAsync(db, hb.data(), hb.size() * 8, cudaMemcpyHostToDevice, st));
   for (int pass = 0; pass < 2; ++pass) {
-    if (pass == 0)
-      WCK(cgemm(cmat<float>(da, M, K, K, 1), cmat<float>(db, K, N, N, 1), cout_<float>(dc, M, N, N, 1), 1.0f, 0.0f,
-                B->gemm, st));
-    else
+    if (pass == 0) {
+      // the tensor-core kernel wherever it takes the product (whatever the
+      // autotuner would pick), else the CUDA-core kernel
+      const cudaError_t e = cgemm_kind(GEMM_TC, cmat<float>(da, M, K, K, 1), cmat<float>(db, K, N, N, 1),
+                                       cout_<float>(dc, M, N, N, 1), 1.0f, 0.0f, B->gemm, st);
+      if (e == cudaErrorInvalidValue) {
+        cudaGetLastError();
+        WCK(cgemm_simt(cmat<float>(da, M, K, K, 1), cmat<float>(db, K, N, N, 1), cout_<float>(dc, M, N, N, 1), 1.0f,
+                       0.0f, st));
+      } else {
+        WCK(e);
+      }
+    } else
       WCK(cgemm_simt(cmat<float>(da, M, K, K, 1), cmat<float>(db, K, N, N, 1), cout_<float>(dc, M, N, N, 1), 1.0f,
                      0.0f, st));
     WCK(cudaMemcpyAsync(hc.data(), dc, hc.size() * 8, cudaMemcpyDeviceToHost, st));
@@ -923,6 +932,70 @@ int wide_diag_cgemm(mps_ctx* c, int M, int N, int K, const double* a, const doub
   WCK(cudaMemcpy(&herr, B->gemm.d_err, sizeof(int), cudaMemcpyDeviceToHost));
   if (herr) return fail(MPS_ERR_TIMEOUT, "tensor-core GEMM wait timed out");
   return MPS_OK;
+}
+
+// One complex product on a chosen GEMM kernel (GemmKind), for tests of
+// every tile shape.  flags: bit 0 stores A column-major, bit 1 stores B
+// column-major, bit 2 writes C column-major, so the kernels' strided loads
+// and stores are exercised; host arrays stay row-major.
+template <typename T>
+static int wide_diag_cgemm_kind_t(mps_ctx* c, int kind, int flags, int M, int N, int K, const double* a,
+                                  const double* b, double* out) {
+  WideBufs* B = nullptr;
+  const int chi = std::max(std::max(M, N), std::max(K, 64));
+  int rc = wide_bufs(&c->wide, sizeof(T) == 8 ? MPS_PREC_FP64 : MPS_PREC_FP32, (chi + 1) / 2 + 64, &B);
+  if (rc) return rc;
+  cudaStream_t st = c->lane0.stream;
+  const bool acm = flags & 1, bcm = flags & 2, ccm = flags & 4;
+  std::vector<cx<T>> ha((size_t)M * K), hb((size_t)K * N), hc((size_t)M * N);
+  for (int i = 0; i < M; ++i)
+    for (int k = 0; k < K; ++k) {
+      const size_t s0 = (size_t)i * K + k;
+      ha[acm ? (size_t)k * M + i : s0] = mk<T>((T)a[2 * s0], (T)a[2 * s0 + 1]);
+    }
+  for (int k = 0; k < K; ++k)
+    for (int j = 0; j < N; ++j) {
+      const size_t s0 = (size_t)k * N + j;
+      hb[bcm ? (size_t)j * K + k : s0] = mk<T>((T)b[2 * s0], (T)b[2 * s0 + 1]);
+    }
+  cx<T>* da = reinterpret_cast<cx<T>*>(B->theta);
+  cx<T>* db = reinterpret_cast<cx<T>*>(B->tbuf);
+  cx<T>* dc = reinterpret_cast<cx<T>*>(B->gram);
+  WCK(cudaMemcpyAsync(da, ha.data(), ha.size() * sizeof(cx<T>), cudaMemcpyHostToDevice, st));
+  WCK(cudaMemcpyAsync(db, hb.data(), hb.size() * sizeof(cx<T>), cudaMemcpyHostToDevice, st));
+  const CMat<T> va = acm ? cmat<T>(da, M, K, 1, M) : cmat<T>(da, M, K, K, 1);
+  const CMat<T> vb = bcm ? cmat<T>(db, K, N, 1, K) : cmat<T>(db, K, N, N, 1);
+  const CMatOut<T> vc = ccm ? cout_<T>(dc, M, N, 1, M) : cout_<T>(dc, M, N, N, 1);
+  const cudaError_t e = cgemm_kind(kind, va, vb, vc, T(1), T(0), B->gemm, st);
+  if (e == cudaErrorInvalidValue) return fail(MPS_ERR_ARG, "this kernel does not take this product");
+  WCK(e);
+  WCK(cudaMemcpyAsync(hc.data(), dc, hc.size() * sizeof(cx<T>), cudaMemcpyDeviceToHost, st));
+  WCK(cudaStreamSynchronize(st));
+  for (int i = 0; i < M; ++i)
+    for (int j = 0; j < N; ++j) {
+      const cx<T> z = hc[ccm ? (size_t)j * M + i : (size_t)i * N + j];
+      out[2 * ((size_t)i * N + j)] = (double)z.re;
+      out[2 * ((size_t)i * N + j) + 1] = (double)z.im;
+    }
+  if (sizeof(T) == 4) {
+    int herr = 0;
+    WCK(cudaMemcpy(&herr, B->gemm.d_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (herr) return fail(MPS_ERR_TIMEOUT, "tensor-core GEMM wait timed out");
+  }
+  return MPS_OK;
+}
+
+int wide_diag_cgemm_kind(mps_ctx* c, int prec, int kind, int flags, int M, int N, int K, const double* a,
+                         const double* b, double* out) {
+  return prec == MPS_PREC_FP64 ? wide_diag_cgemm_kind_t<double>(c, kind, flags, M, N, K, a, b, out)
+                               : wide_diag_cgemm_kind_t<float>(c, kind, flags, M, N, K, a, b, out);
+}
+
+int wide_gemm_tunings(mps_ctx* c) {
+  int n = 0;
+  if (!c->wide) return 0;
+  for (auto& b : reinterpret_cast<WideAll*>(c->wide)->b) n += b.gemm.tunings;
+  return n;
 }
 
 }  // namespace gbmps

@@ -63,6 +63,17 @@ inline CMatOut<T> cout_(void* p, int rows, int cols, int64_t rs, int64_t cs) {
   return v;
 }
 
+// Kernels a complex GEMM can run on: CUDA-core tiles of rows x columns of
+// complex outputs per CTA, and (complex64 only) the tensor-core kernel.
+enum GemmKind {
+  GEMM_SIMT_64x64 = 0,
+  GEMM_SIMT_32x32 = 1,
+  GEMM_SIMT_16x64 = 2,
+  GEMM_SIMT_64x16 = 3,
+  GEMM_TC = 4,
+  GEMM_KINDS = 5
+};
+
 // Device workspace of the GEMMs: the split (hi/lo) real-embedded operands of
 // the tensor-core path.  Sized for the largest wide product.
 struct GemmWs {
@@ -74,6 +85,11 @@ struct GemmWs {
   int* d_err = nullptr;  // barrier/wait time-outs of the tensor-core kernel
   int tc_launches = 0;   // tensor-core GEMM launches issued (diagnostics)
   int simt_launches = 0;
+  // autotuner: output buffer of the trial launches and their timing events
+  void* tune_c = nullptr;
+  size_t tune_c_bytes = 0;
+  cudaEvent_t tune_ev[2] = {nullptr, nullptr};
+  int tunings = 0;  // shape buckets tuned with this workspace
 };
 int gemm_ws_init(GemmWs& ws, size_t a_elems, size_t b_elems);
 void gemm_ws_free(GemmWs& ws);
@@ -89,6 +105,28 @@ cudaError_t cgemm(const CMat<double>& A, const CMat<double>& B, const CMatOut<do
 // Force the CUDA-core kernel (cross-checks of the tensor-core path).
 cudaError_t cgemm_simt(const CMat<float>& A, const CMat<float>& B, const CMatOut<float>& C, float alpha,
                        float beta, cudaStream_t st);
+// Run one given kernel (GemmKind); GEMM_TC only for complex64 products the
+// tensor-core kernel accepts (else cudaErrorInvalidValue).
+cudaError_t cgemm_kind(int kind, const CMat<float>& A, const CMat<float>& B, const CMatOut<float>& C, float alpha,
+                       float beta, GemmWs& ws, cudaStream_t st);
+cudaError_t cgemm_kind(int kind, const CMat<double>& A, const CMat<double>& B, const CMatOut<double>& C,
+                       double alpha, double beta, GemmWs& ws, cudaStream_t st);
+
+// GEMM autotuner.  Products are grouped into buckets by device, precision,
+// ceil(log2) of M, N and K, and which index of A, B and C is unit-stride.
+// Mode 0 uses the static rule (tensor cores for complex64 products of at
+// least ~2M complex MACs, else 64 x 64 CUDA-core tiles); mode 1 times every
+// eligible kernel on the first product of a new bucket (trial launches write
+// a scratch output, the inputs are only read) and keeps the fastest; mode 2
+// uses tuned or loaded entries without tuning new buckets.  The table is
+// shared by every context of the process.
+constexpr int kTuneCols = 9;  // device, prec, lg M, lg N, lg K, layout, kernel, ns, ns of the static rule
+void gemm_tune_set_mode(int mode);
+int gemm_tune_mode();
+int gemm_tune_table(int* out, int cap);
+int gemm_tune_save(const char* path);
+int gemm_tune_load(const char* path);
+void gemm_tune_clear();
 
 // ------------------------------------------------------------ cooperative
 constexpr int32_t kCoopTimeout = 1 << 8;

@@ -19,6 +19,11 @@ PREC_FP64, PREC_FP32 = 0, 1
 FLAG_RENORM, FLAG_PER_GATE, FLAG_SWEEP = 1, 2, 4
 CHI_LIMIT = 64
 WIDE_CHI_LIMIT = 1024
+# GEMM kernels of the wide path (MPS_GEMM_*) and the autotuner's row width
+GEMM_SIMT_64x64, GEMM_SIMT_32x32, GEMM_SIMT_16x64, GEMM_SIMT_64x16, GEMM_TC = range(5)
+GEMM_KERNEL_NAMES = ["simt64x64", "simt32x32", "simt16x64", "simt64x16", "tc"]
+AUTOTUNE_COLS = 9
+AUTOTUNE_FIELDS = ("device", "precision", "lg_m", "lg_n", "lg_k", "layout", "kernel", "ns", "static_ns")
 
 _ERR_NAMES = {1: "MPS_ERR_ARG", 2: "MPS_ERR_OOM", 3: "MPS_ERR_TIMEOUT", 4: "MPS_ERR_NUMERIC",
               5: "MPS_ERR_CUDA", 6: "MPS_ERR_STATE", 7: "MPS_ERR_UNSUPPORTED"}
@@ -75,6 +80,15 @@ SIGNATURES = [
                                             _P, _c.POINTER(_c.c_int), _DP, _P]),
     ("mps_diag_cgemm", _c.c_int, [_P, _c.c_int, _c.c_int, _c.c_int, _DP, _DP, _DP, _DP]),
     ("mps_diag_gemm_counts", _c.c_int, [_P, _c.POINTER(_c.c_int), _c.POINTER(_c.c_int)]),
+    ("mps_diag_cgemm_kind", _c.c_int, [_P, _c.c_int, _c.c_int, _c.c_int, _c.c_int, _c.c_int, _c.c_int, _DP, _DP,
+                                        _DP]),
+    ("mps_autotune_set_mode", _c.c_int, [_c.c_int]),
+    ("mps_autotune_get_mode", _c.c_int, [_c.POINTER(_c.c_int)]),
+    ("mps_autotune_table", _c.c_int, [_c.POINTER(_c.c_int), _c.c_int, _c.POINTER(_c.c_int)]),
+    ("mps_autotune_save", _c.c_int, [_c.c_char_p]),
+    ("mps_autotune_load", _c.c_int, [_c.c_char_p]),
+    ("mps_autotune_clear", _c.c_int, []),
+    ("mps_autotune_tunings", _c.c_int, [_P, _c.POINTER(_c.c_int)]),
 ]
 
 GATE_IDS = {name: i for i, name in enumerate(
@@ -221,6 +235,67 @@ class Context:
         t, s = ctypes.c_int(), ctypes.c_int()
         _check(_lib.mps_diag_gemm_counts(self.h, ctypes.byref(t), ctypes.byref(s)))
         return t.value, s.value
+
+    def diag_cgemm_kind(self, a, b, kernel, precision=PREC_FP32, flags=0):
+        """a @ b on one chosen GEMM kernel (GEMM_*) in complex64 or complex128;
+        flags bits 0/1/2 store A/B/C column-major on the device."""
+        a = np.ascontiguousarray(a, dtype=np.complex128)
+        b = np.ascontiguousarray(b, dtype=np.complex128)
+        M, K = a.shape
+        N = b.shape[1]
+        c = np.zeros((M, N), dtype=np.complex128)
+        _check(_lib.mps_diag_cgemm_kind(self.h, precision, kernel, flags, M, N, K, _dptr(a.view(np.float64)),
+                                        _dptr(b.view(np.float64)), _dptr(c.view(np.float64))))
+        return c
+
+    def autotune_tunings(self):
+        """Shape buckets tuned by this context's wide workspaces so far."""
+        n = ctypes.c_int()
+        _check(_lib.mps_autotune_tunings(self.h, ctypes.byref(n)))
+        return n.value
+
+
+# ---- GEMM autotuner of the wide path (process-wide table)
+def autotune_set_mode(mode):
+    """0 static rule, 1 tune new shape buckets, 2 tuned/loaded entries only."""
+    load_library()
+    _check(_lib.mps_autotune_set_mode(mode))
+
+
+def autotune_mode():
+    load_library()
+    m = ctypes.c_int()
+    _check(_lib.mps_autotune_get_mode(ctypes.byref(m)))
+    return m.value
+
+
+def autotune_table():
+    """List of dicts, one per tuned bucket (fields AUTOTUNE_FIELDS)."""
+    load_library()
+    n = ctypes.c_int()
+    _check(_lib.mps_autotune_table(None, 0, ctypes.byref(n)))
+    cap = n.value
+    buf = (ctypes.c_int * max(1, cap * AUTOTUNE_COLS))()
+    _check(_lib.mps_autotune_table(buf, cap, ctypes.byref(n)))
+    rows = []
+    for i in range(min(cap, n.value)):
+        rows.append(dict(zip(AUTOTUNE_FIELDS, buf[i * AUTOTUNE_COLS:(i + 1) * AUTOTUNE_COLS])))
+    return rows
+
+
+def autotune_save(path):
+    load_library()
+    _check(_lib.mps_autotune_save(os.fsencode(path)))
+
+
+def autotune_load(path):
+    load_library()
+    _check(_lib.mps_autotune_load(os.fsencode(path)))
+
+
+def autotune_clear():
+    load_library()
+    _check(_lib.mps_autotune_clear())
 
 
 class Graph:
