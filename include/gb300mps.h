@@ -257,8 +257,9 @@ int mps_diag_gemm_counts(mps_ctx* ctx, int* tensor_core, int* cuda_core);
  * tensor-core kernel differs from them by FP32 rounding (~1e-6 relative).
  * Tuning synchronises the stream and allocates a 64 MiB scratch buffer per
  * workspace once, so it is skipped inside a stream capture.  The initial
- * mode comes from the environment variable GB300MPS_AUTOTUNE (default 0).
- * The table is process-wide. */
+ * mode comes from the environment variable GB300MPS_AUTOTUNE (default 1).
+ * The table is process-wide.  For run-to-run identical complex64 results use
+ * mode 0, or mode 2 with a loaded table. */
 #define MPS_AUTOTUNE_COLS 9
 int mps_autotune_set_mode(int mode);
 int mps_autotune_get_mode(int* mode);

@@ -510,7 +510,7 @@ struct TuneEntry {
 
 std::mutex g_tune_mu;
 std::map<uint32_t, TuneEntry> g_tune;
-int g_tune_mode = -1;  // -1: not read from the environment yet
+int g_tune_mode = -1;  // -1: not read from the environment yet (default 1, tune)
 
 constexpr size_t kTuneMaxBytes = size_t(64) << 20;  // largest trial output (64 MiB)
 constexpr int kTuneReps = 3;                         // timed launches per kernel after one warm-up
@@ -538,8 +538,8 @@ int mode_now() {
   std::lock_guard<std::mutex> lk(g_tune_mu);
   if (g_tune_mode < 0) {
     const char* e = getenv("GB300MPS_AUTOTUNE");
-    g_tune_mode = (e && *e) ? atoi(e) : 0;
-    if (g_tune_mode < 0 || g_tune_mode > 2) g_tune_mode = 0;
+    g_tune_mode = (e && *e) ? atoi(e) : 1;
+    if (g_tune_mode < 0 || g_tune_mode > 2) g_tune_mode = 1;
   }
   return g_tune_mode;
 }

@@ -119,7 +119,8 @@ cudaError_t cgemm_kind(int kind, const CMat<double>& A, const CMat<double>& B, c
 // eligible kernel on the first product of a new bucket (trial launches write
 // a scratch output, the inputs are only read) and keeps the fastest; mode 2
 // uses tuned or loaded entries without tuning new buckets.  The table is
-// shared by every context of the process.
+// shared by every context of the process; the initial mode is 1 unless the
+// environment variable GB300MPS_AUTOTUNE names another.
 constexpr int kTuneCols = 9;  // device, prec, lg M, lg N, lg K, layout, kernel, ns, ns of the static rule
 void gemm_tune_set_mode(int mode);
 int gemm_tune_mode();
