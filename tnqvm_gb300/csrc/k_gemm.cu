@@ -711,7 +711,7 @@ int gemm_tune_save(const char* path) {
   fprintf(f, "# gb300mps gemm tuning v1: key kind static_kind ns[%d]\n", (int)GEMM_KINDS);
   for (const auto& kv : g_tune) {
     fprintf(f, "%u %d %d", kv.first, kv.second.kind, kv.second.static_kind);
-    for (float t : kv.second.ns) fprintf(f, " %.1f", t);
+    for (float t : kv.second.ns) fprintf(f, " %.9g", (double)t);  // exact float round trip
     fprintf(f, "\n");
   }
   return fclose(f) == 0 ? 0 : 1;

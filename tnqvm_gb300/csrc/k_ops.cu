@@ -504,6 +504,46 @@ __device__ void tri_backtransform(const cx<T>* A, cx<T>* W, int m, int k, int ld
   }
 }
 
+// C (R x Q) = A B with A(r, l), B(l, q) given by functors, in register
+// tiles of TR x TQ outputs per thread (threads take tiles with q fastest, so a
+// warp reads B contiguously and A as a broadcast).  Each output sums l = 0 ..
+// K-1 in order with fma_c, as the untiled loops do; store(r, q, value).
+template <typename T, int TR, int TQ, typename FA, typename FB, typename FS>
+__device__ __forceinline__ void tiled_product(int R, int Q, int K, FA fa, FB fb, FS store) {
+  const int nr = (R + TR - 1) / TR, nq = (Q + TQ - 1) / TQ;
+  for (int tt = threadIdx.x; tt < nr * nq; tt += blockDim.x) {
+    const int tr = tt / nq, tq = tt - tr * nq;
+    int rr[TR], qq[TQ];
+#pragma unroll
+    for (int a = 0; a < TR; ++a) rr[a] = min(TR * tr + a, R - 1);
+#pragma unroll
+    for (int b = 0; b < TQ; ++b) qq[b] = min(TQ * tq + b, Q - 1);
+    cx<T> acc[TR][TQ];
+#pragma unroll
+    for (int a = 0; a < TR; ++a)
+#pragma unroll
+      for (int b = 0; b < TQ; ++b) acc[a][b] = mk<T>(0, 0);
+    for (int l = 0; l < K; ++l) {
+      cx<T> x[TR], y[TQ];
+#pragma unroll
+      for (int a = 0; a < TR; ++a) x[a] = fa(rr[a], l);
+#pragma unroll
+      for (int b = 0; b < TQ; ++b) y[b] = fb(l, qq[b]);
+#pragma unroll
+      for (int a = 0; a < TR; ++a)
+#pragma unroll
+        for (int b = 0; b < TQ; ++b) fma_c(acc[a][b], x[a], y[b]);
+    }
+#pragma unroll
+    for (int a = 0; a < TR; ++a)
+#pragma unroll
+      for (int b = 0; b < TQ; ++b) {
+        const int r = TR * tr + a, q = TQ * tq + b;
+        if (r < R && q < Q) store(r, q, acc[a][b]);
+      }
+  }
+}
+
 // Orthonormalise the columns of Wc (m x k, ld k).  Newton-Schulz steps
 // W <- W - 1/2 W (W^H W - I) remove rounding from the orthonormality (each
 // step squares the defect; W W^H is a projector only to that defect, so steps
@@ -521,13 +561,46 @@ __device__ const cx<T>* orthonormalize(cx<T>* Wc, int m, int k, cx<T>* U, SmallS
   for (int it = 0; it < 5; ++it) {
     __syncthreads();
     T f2 = T(0);
-    for (int t = tid; t < k * k; t += nt) {
-      const int a = t / k, b = t - a * k;
-      cx<T> acc = mk<T>(0, 0);
-      for (int i = 0; i < m; ++i) fma_cj(acc, cur[i * k + a], cur[i * k + b]);
-      if (a == b) acc.re -= T(1);
-      E[t] = acc;
-      f2 += abs2(acc);
+    {
+      // E = W^H W - I in 2 x 4 register tiles (each entry sums over rows in order)
+      const int nta = (k + 1) >> 1, ntb = (k + 3) >> 2;
+      for (int tt = tid; tt < nta * ntb; tt += nt) {
+        const int ta = tt / ntb, tb = tt - ta * ntb;
+        int ca[2], cb[4];
+#pragma unroll
+        for (int a = 0; a < 2; ++a) ca[a] = min(2 * ta + a, k - 1);
+#pragma unroll
+        for (int b = 0; b < 4; ++b) cb[b] = min(4 * tb + b, k - 1);
+        cx<T> acc[2][4];
+#pragma unroll
+        for (int a = 0; a < 2; ++a)
+#pragma unroll
+          for (int b = 0; b < 4; ++b) acc[a][b] = mk<T>(0, 0);
+        for (int i = 0; i < m; ++i) {
+          const cx<T>* row = cur + i * k;
+          cx<T> xa[2], xb[4];
+#pragma unroll
+          for (int a = 0; a < 2; ++a) xa[a] = row[ca[a]];
+#pragma unroll
+          for (int b = 0; b < 4; ++b) xb[b] = row[cb[b]];
+#pragma unroll
+          for (int a = 0; a < 2; ++a)
+#pragma unroll
+            for (int b = 0; b < 4; ++b) fma_cj(acc[a][b], xa[a], xb[b]);
+        }
+#pragma unroll
+        for (int a = 0; a < 2; ++a)
+#pragma unroll
+          for (int b = 0; b < 4; ++b) {
+            const int ea = 2 * ta + a, eb = 4 * tb + b;
+            if (ea < k && eb < k) {
+              cx<T> v = acc[a][b];
+              if (ea == eb) v.re -= T(1);
+              E[ea * k + eb] = v;
+              f2 += abs2(v);
+            }
+          }
+      }
     }
     // |E|_2 <= |E|_F: below 0.1 the steps converge quadratically
     const double fro = sqrt((double)block_sum<T>(f2, sm->red));
@@ -537,11 +610,41 @@ __device__ const cx<T>* orthonormalize(cx<T>* Wc, int m, int k, cx<T>* U, SmallS
       __syncthreads();
       return Wc;
     }
-    for (int t = tid; t < m * k; t += nt) {
-      const int i = t / k, j = t - i * k;
-      cx<T> corr = mk<T>(0, 0);
-      for (int l = 0; l < k; ++l) fma_c(corr, cur[i * k + l], E[l * k + j]);
-      nxt[t] = cur[t] - scl(corr, T(0.5));
+    {
+      // W - 1/2 W E in UR x 4 register tiles (each entry sums over l in order)
+      constexpr int UR = sizeof(T) == 4 ? 4 : 2;
+      const int nti = (m + UR - 1) / UR, ntj = (k + 3) >> 2;
+      for (int tt = tid; tt < nti * ntj; tt += nt) {
+        const int ti = tt / ntj, tj = tt - ti * ntj;
+        int ri[UR], cj[4];
+#pragma unroll
+        for (int a = 0; a < UR; ++a) ri[a] = min(UR * ti + a, m - 1) * k;
+#pragma unroll
+        for (int b = 0; b < 4; ++b) cj[b] = min(4 * tj + b, k - 1);
+        cx<T> corr[UR][4];
+#pragma unroll
+        for (int a = 0; a < UR; ++a)
+#pragma unroll
+          for (int b = 0; b < 4; ++b) corr[a][b] = mk<T>(0, 0);
+        for (int l = 0; l < k; ++l) {
+          cx<T> xa[UR], eb[4];
+#pragma unroll
+          for (int a = 0; a < UR; ++a) xa[a] = cur[ri[a] + l];
+#pragma unroll
+          for (int b = 0; b < 4; ++b) eb[b] = E[l * k + cj[b]];
+#pragma unroll
+          for (int a = 0; a < UR; ++a)
+#pragma unroll
+            for (int b = 0; b < 4; ++b) fma_c(corr[a][b], xa[a], eb[b]);
+        }
+#pragma unroll
+        for (int a = 0; a < UR; ++a)
+#pragma unroll
+          for (int b = 0; b < 4; ++b) {
+            const int i = UR * ti + a, j = 4 * tj + b;
+            if (i < m && j < k) nxt[i * k + j] = cur[i * k + j] - scl(corr[a][b], T(0.5));
+          }
+      }
     }
     __syncthreads();
     cx<T>* tmp = cur;
@@ -930,19 +1033,14 @@ __device__ void op_gate2(const ProgDesc& P, const DevOp& op, char* big, SmallSme
       cx<T>* Yv = Wg + kMaxM * kChiLimit;  // X^H W (nn x k)
       for (int t = tid; t < m * k; t += nt) Wk[t] = W[t];
       __syncthreads();
-      for (int t = tid; t < nn * k; t += nt) {
-        const int c = t / k, j = t - c * k;
-        cx<T> acc = mk<T>(0, 0);
-        for (int i = 0; i < m; ++i) fma_cj(acc, X(i, c), Wk[i * k + j]);
-        Yv[t] = acc;
-      }
+      constexpr int TR = sizeof(T) == 4 ? 4 : 2;
+      tiled_product<T, TR, 4>(
+          nn, k, m, [&](int c, int i) { return conj(X(i, c)); }, [&](int i, int j) { return Wk[i * k + j]; },
+          [&](int c, int j, cx<T> v) { Yv[c * k + j] = v; });
       __syncthreads();
-      for (int t = tid; t < m * k; t += nt) {
-        const int i = t / k, j = t - i * k;
-        cx<T> acc = mk<T>(0, 0);
-        for (int c = 0; c < nn; ++c) fma_c(acc, X(i, c), Yv[c * k + j]);
-        Wc[t] = acc;
-      }
+      tiled_product<T, TR, 4>(
+          m, k, nn, [&](int i, int c) { return X(i, c); }, [&](int c, int j) { return Yv[c * k + j]; },
+          [&](int i, int j, cx<T> v) { Wc[i * k + j] = v; });
       __syncthreads();
       for (int j = tid; j < k; j += nt) {
         T s2 = T(0);
@@ -962,15 +1060,17 @@ __device__ void op_gate2(const ProgDesc& P, const DevOp& op, char* big, SmallSme
   cyc_vec += c_orth - c_vec;
   cyc_orth += clock64() - c_orth;
   // other side: Z = W_k^H X (k x nn)
-  for (int t = tid; t < k * nn; t += nt) {
-    const int j = t / nn, c = t - j * nn;
-    cx<T> acc = mk<T>(0, 0);
-    for (int i = 0; i < m; ++i) fma_cj(acc, W[i * k + j], X(i, c));
-    acc = scl(acc, sm->oth[j]);
-    if (!tr)
-      B[j * Cc + c] = acc;  // hi site (k, 2, dr)
-    else
-      A[c * k + j] = acc;   // lo site (dl, 2, k)
+  {
+    constexpr int TR = sizeof(T) == 4 ? 4 : 2;
+    tiled_product<T, TR, 4>(
+        k, nn, m, [&](int j, int i) { return conj(W[i * k + j]); }, [&](int i, int c) { return X(i, c); },
+        [&](int j, int c, cx<T> v) {
+          const cx<T> acc = scl(v, sm->oth[j]);
+          if (!tr)
+            B[j * Cc + c] = acc;  // hi site (k, 2, dr)
+          else
+            A[c * k + j] = acc;   // lo site (dl, 2, k)
+        });
   }
   // isometric side: W_k
   for (int t = tid; t < m * k; t += nt) {
