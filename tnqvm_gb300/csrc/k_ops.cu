@@ -121,7 +121,8 @@ struct Layout {
   static constexpr size_t gram_bytes = sizeof(cx<T>) * (kMaxM * (kMaxM + 1) / 2);
   // U (m x m), or X staged for the Gram with a padded stride (m x (m+1))
   static constexpr size_t u_bytes = Prec<T>::u_in_smem ? sizeof(cx<T>) * kMaxM * (kMaxM + 1) : 0;
-  static constexpr size_t qr_bytes = sizeof(cx<T>) * (kMaxM * kChiLimit + kChiLimit * kChiLimit);
+  // QR of a centre move: M (<= kMaxM x kChiLimit, odd row stride <= kChiLimit + 1), then R
+  static constexpr size_t qr_bytes = sizeof(cx<T>) * (kMaxM * (kChiLimit + 1) + kChiLimit * kChiLimit);
   static constexpr size_t big = (gram_bytes + u_bytes) > qr_bytes ? (gram_bytes + u_bytes) : qr_bytes;
   static constexpr size_t smem = big + sizeof(SmallSmem<T>);
   // Global scratch per CTA: theta, then the eigensolver's work matrix for
@@ -131,16 +132,22 @@ struct Layout {
       sizeof(cx<T>) * (kMaxM * kMaxM + (Prec<T>::u_in_smem ? 2 * kMaxM * kChiLimit : kMaxM * kMaxM));
 };
 
+static_assert(Layout<float>::smem <= 232448 && Layout<double>::smem <= 232448,
+              "the fused kernel's shared memory must fit one CTA's 227 KB");
+
 // FP32 refinement threshold: eigenvalues below this fraction of the largest
 // form the tail that is re-solved (singular-value ratio 1e-2; the FP32 Gram's
 // absolute error is ~1e-7 of the trace).
 constexpr double kRefineRatio = 1e-4;
 
 // ---------------------------------------------------------- Householder QR
-// M (mr x nc, ld = nc) -> Q in the first k = min(mr,nc) columns of M,
-// R (k x nc, ld = nc) in Rb.  Same reflector convention as LAPACK zgeqr2/zung2r.
+// M (mr x nc, row stride ld >= nc) -> Q in the first k = min(mr,nc) columns
+// of M, R (k x nc, ld = nc) in Rb.  Same reflector convention as LAPACK
+// zgeqr2/zung2r.  Lanes walk a column's rows, so an odd ld keeps those
+// shared-memory loads free of bank conflicts (an ld that is a multiple of 16
+// puts all 32 lanes on one bank).
 template <typename T>
-__device__ void householder_qr(cx<T>* M, int mr, int nc, cx<T>* Rb, SmallSmem<T>* sm) {
+__device__ void householder_qr(cx<T>* M, int mr, int nc, int ld, cx<T>* Rb, SmallSmem<T>* sm) {
   const int tid = threadIdx.x, nt = blockDim.x;
   const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
   const int k = mr < nc ? mr : nc;
@@ -148,9 +155,9 @@ __device__ void householder_qr(cx<T>* M, int mr, int nc, cx<T>* Rb, SmallSmem<T>
     // warp 0: norm, reflector scalars (working precision) and the scaled column
     if (warp == 0) {
       T s = T(0);
-      for (int i = j + 1 + lane; i < mr; i += 32) s += abs2(M[i * nc + j]);
+      for (int i = j + 1 + lane; i < mr; i += 32) s += abs2(M[i * ld + j]);
       for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-      const cx<T> alpha = M[j * nc + j];
+      const cx<T> alpha = M[j * ld + j];
       __syncwarp();  // every lane has read alpha before lane 0 overwrites it with beta
       const T ar = alpha.re, ai = alpha.im;
       const T nrm2 = ar * ar + ai * ai + s;
@@ -164,11 +171,11 @@ __device__ void householder_qr(cx<T>* M, int mr, int nc, cx<T>* Rb, SmallSmem<T>
         ii = -di / den;
         if (lane == 0) {
           sm->tau[j] = mk<T>((beta - ar) / beta, -ai / beta);
-          M[j * nc + j] = mk<T>(beta, T(0));
+          M[j * ld + j] = mk<T>(beta, T(0));
         }
         for (int i = j + 1 + lane; i < mr; i += 32) {
-          const cx<T> x = M[i * nc + j];
-          M[i * nc + j] = mk<T>(x.re * ir - x.im * ii, x.re * ii + x.im * ir);
+          const cx<T> x = M[i * ld + j];
+          M[i * ld + j] = mk<T>(x.re * ir - x.im * ii, x.re * ii + x.im * ir);
         }
       } else if (lane == 0) {
         sm->tau[j] = mk<T>(0, 0);
@@ -180,23 +187,23 @@ __device__ void householder_qr(cx<T>* M, int mr, int nc, cx<T>* Rb, SmallSmem<T>
       const cx<T> ctau = conj(sm->tau[j]);
       for (int c = j + 1 + warp; c < nc; c += nw) {
         cx<T> w = mk<T>(0, 0);
-        for (int i = j + 1 + lane; i < mr; i += 32) fma_cj(w, M[i * nc + j], M[i * nc + c]);
+        for (int i = j + 1 + lane; i < mr; i += 32) fma_cj(w, M[i * ld + j], M[i * ld + c]);
         for (int o = 16; o > 0; o >>= 1) {
           w.re += __shfl_xor_sync(0xffffffffu, w.re, o);
           w.im += __shfl_xor_sync(0xffffffffu, w.im, o);
         }
-        w = w + M[j * nc + c];
+        w = w + M[j * ld + c];
         const cx<T> tw = ctau * w;
-        for (int i = j + 1 + lane; i < mr; i += 32) M[i * nc + c] = M[i * nc + c] - M[i * nc + j] * tw;
+        for (int i = j + 1 + lane; i < mr; i += 32) M[i * ld + c] = M[i * ld + c] - M[i * ld + j] * tw;
         __syncwarp();
-        if (lane == 0) M[j * nc + c] = M[j * nc + c] - tw;
+        if (lane == 0) M[j * ld + c] = M[j * ld + c] - tw;
       }
     }
     __syncthreads();
   }
   for (int t = tid; t < k * nc; t += nt) {
     const int i = t / nc, c = t - i * nc;
-    Rb[t] = c >= i ? M[i * nc + c] : mk<T>(0, 0);
+    Rb[t] = c >= i ? M[i * ld + c] : mk<T>(0, 0);
   }
   __syncthreads();
   for (int j = k - 1; j >= 0; --j) {
@@ -204,26 +211,26 @@ __device__ void householder_qr(cx<T>* M, int mr, int nc, cx<T>* Rb, SmallSmem<T>
     if (j < k - 1 && (tj.re != T(0) || tj.im != T(0))) {
       for (int c = j + 1 + warp; c < k; c += nw) {
         cx<T> w = mk<T>(0, 0);
-        for (int i = j + 1 + lane; i < mr; i += 32) fma_cj(w, M[i * nc + j], M[i * nc + c]);
+        for (int i = j + 1 + lane; i < mr; i += 32) fma_cj(w, M[i * ld + j], M[i * ld + c]);
         for (int o = 16; o > 0; o >>= 1) {
           w.re += __shfl_xor_sync(0xffffffffu, w.re, o);
           w.im += __shfl_xor_sync(0xffffffffu, w.im, o);
         }
-        w = w + M[j * nc + c];
+        w = w + M[j * ld + c];
         const cx<T> tw = tj * w;
-        for (int i = j + 1 + lane; i < mr; i += 32) M[i * nc + c] = M[i * nc + c] - M[i * nc + j] * tw;
+        for (int i = j + 1 + lane; i < mr; i += 32) M[i * ld + c] = M[i * ld + c] - M[i * ld + j] * tw;
         __syncwarp();
-        if (lane == 0) M[j * nc + c] = M[j * nc + c] - tw;
+        if (lane == 0) M[j * ld + c] = M[j * ld + c] - tw;
       }
     }
     __syncthreads();
     for (int i = tid; i < mr; i += nt) {
       if (i > j)
-        M[i * nc + j] = mk<T>(T(0), T(0)) - tj * M[i * nc + j];
+        M[i * ld + j] = mk<T>(T(0), T(0)) - tj * M[i * ld + j];
       else if (i == j)
-        M[i * nc + j] = mk<T>(T(1) - tj.re, -tj.im);
+        M[i * ld + j] = mk<T>(T(1) - tj.re, -tj.im);
       else
-        M[i * nc + j] = mk<T>(0, 0);
+        M[i * ld + j] = mk<T>(0, 0);
     }
     __syncthreads();
   }
@@ -236,12 +243,22 @@ __device__ void householder_qr(cx<T>* M, int mr, int nc, cx<T>* Rb, SmallSmem<T>
 // eigenvectors by one twisted factorisation each (Dhillon-Parlett), and the
 // back-transform by the stored reflectors.
 
-// A: full Hermitian m x m (ld m) in shared memory.  On return td/te hold the
+// Row stride of the eigensolver's m x m work matrix: odd in shared memory
+// (FP32), so column walks and the four-lanes-per-row products of the
+// tridiagonalisation are free of bank conflicts; m in global memory (FP64),
+// whose scratch holds exactly m x m.
+template <typename T>
+__device__ __forceinline__ int eig_ld(int m) {
+  return Prec<T>::u_in_smem ? (m | 1) : m;
+}
+
+// A: full Hermitian m x m (row stride eig_ld(m)) in shared memory.  On return td/te hold the
 // tridiagonal T = Q^H A Q, Q = H_0 ... H_{m-2}, H_j = I - ttau[j] v_j v_j^H with
 // v_j[j+1] = 1 and v_j[i] (i > j+1) stored in A[i][j] (LAPACK zhetd2, lower).
 template <typename T>
 __device__ void tridiagonalize(cx<T>* A, int m, double trace, SmallSmem<T>* sm) {
   const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
+  const int lda = eig_ld<T>(m);
   // columns this small relative to the trace carry eigen-weight below the
   // working precision; they are flushed to zero so 1/(alpha - beta) stays finite
   const T flush2 = T(Prec<T>::tri_flush * trace * trace + Prec<T>::tiny);
@@ -250,9 +267,9 @@ __device__ void tridiagonalize(cx<T>* A, int m, double trace, SmallSmem<T>* sm) 
     // warp 0: reflector of column j (scalars in working precision)
     if (warp == 0) {
       T s = T(0);
-      for (int i = 1 + lane; i < L; i += 32) s += abs2(A[(j + 1 + i) * m + j]);
+      for (int i = 1 + lane; i < L; i += 32) s += abs2(A[(j + 1 + i) * lda + j]);
       for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-      const cx<T> alpha = A[(j + 1) * m + j];
+      const cx<T> alpha = A[(j + 1) * lda + j];
       const T ar = alpha.re, ai = alpha.im;
       const T nrm2 = ar * ar + ai * ai + s;
       const bool flush = nrm2 <= flush2;
@@ -269,7 +286,7 @@ __device__ void tridiagonalize(cx<T>* A, int m, double trace, SmallSmem<T>* sm) 
       for (int i = lane; i < L; i += 32) {
         cx<T> v = mk<T>(T(i == 0), T(0));
         if (i > 0 && refl) {
-          const cx<T> x = A[(j + 1 + i) * m + j];
+          const cx<T> x = A[(j + 1 + i) * lda + j];
           v = mk<T>(x.re * ir - x.im * ii, x.re * ii + x.im * ir);
         }
         sm->tv[i] = v;
@@ -281,7 +298,7 @@ __device__ void tridiagonalize(cx<T>* A, int m, double trace, SmallSmem<T>* sm) 
     }
     __syncthreads();
     const cx<T> tau = sm->ttau[j];
-    for (int i = tid; i < L; i += nt) A[(j + 1 + i) * m + j] = i == 0 ? mk<T>(sm->te[j], 0) : sm->tv[i];
+    for (int i = tid; i < L; i += nt) A[(j + 1 + i) * lda + j] = i == 0 ? mk<T>(sm->te[j], 0) : sm->tv[i];
     if (tau.re == T(0) && tau.im == T(0)) {
       __syncthreads();
       continue;
@@ -291,7 +308,7 @@ __device__ void tridiagonalize(cx<T>* A, int m, double trace, SmallSmem<T>* sm) 
       const int r = tid >> 2, q = tid & 3;
       cx<T> acc = mk<T>(0, 0);
       if (r < L) {
-        const cx<T>* row = A + (j + 1 + r) * m + (j + 1);
+        const cx<T>* row = A + (j + 1 + r) * lda + (j + 1);
         for (int c = q; c < L; c += 4) fma_c(acc, row[c], sm->tv[c]);
       }
       acc.re += __shfl_xor_sync(0xffffffffu, acc.re, 1);
@@ -322,13 +339,13 @@ __device__ void tridiagonalize(cx<T>* A, int m, double trace, SmallSmem<T>* sm) 
         const int r = t / L, c = t - r * L;
         const cx<T> vr = sm->tv[r], vc = sm->tv[c];
         const cx<T> wr = sm->tp[r] + a2 * vr, wc = sm->tp[c] + a2 * vc;
-        cx<T>& a = A[(j + 1 + r) * m + (j + 1 + c)];
+        cx<T>& a = A[(j + 1 + r) * lda + (j + 1 + c)];
         a = a - (vr * conj(wc) + wr * conj(vc));
       }
     }
     __syncthreads();
   }
-  for (int i = tid; i < m; i += nt) sm->td[i] = A[i * m + i].re;
+  for (int i = tid; i < m; i += nt) sm->td[i] = A[i * lda + i].re;
   __syncthreads();
 }
 
@@ -484,6 +501,7 @@ __device__ void tri_twisted(cx<T>* W, int m, int k, int c, T lam, int s, int t, 
 template <typename T>
 __device__ void tri_backtransform(const cx<T>* A, cx<T>* W, int m, int k, int ld, SmallSmem<T>* sm) {
   const int tid = threadIdx.x, nt = blockDim.x;
+  const int lda = eig_ld<T>(m);
   for (int j = m - 2; j >= 0; --j) {
     const cx<T> tau = sm->ttau[j];
     if (tau.re == T(0) && tau.im == T(0)) continue;
@@ -491,13 +509,13 @@ __device__ void tri_backtransform(const cx<T>* A, cx<T>* W, int m, int k, int ld
     // v^H W for each column: serial over rows, one thread per column (k <= 64)
     for (int c = tid; c < k; c += nt) {
       cx<T> acc = W[(j + 1) * ld + c];
-      for (int i = 1; i < L; ++i) fma_cj(acc, A[(j + 1 + i) * m + j], W[(j + 1 + i) * ld + c]);
+      for (int i = 1; i < L; ++i) fma_cj(acc, A[(j + 1 + i) * lda + j], W[(j + 1 + i) * ld + c]);
       sm->twv[c] = tau * acc;
     }
     __syncthreads();
     for (int t = tid; t < L * k; t += nt) {
       const int i = t / k, c = t - i * k;
-      const cx<T> v = i == 0 ? mk<T>(1, 0) : A[(j + 1 + i) * m + j];
+      const cx<T> v = i == 0 ? mk<T>(1, 0) : A[(j + 1 + i) * lda + j];
       W[(j + 1 + i) * ld + c] = W[(j + 1 + i) * ld + c] - v * sm->twv[c];
     }
     __syncthreads();
@@ -605,7 +623,7 @@ __device__ const cx<T>* orthonormalize(cx<T>* Wc, int m, int k, cx<T>* U, SmallS
     // |E|_2 <= |E|_F: below 0.1 the steps converge quadratically
     const double fro = sqrt((double)block_sum<T>(f2, sm->red));
     if (it == 0 && fro > 0.1) {
-      householder_qr<T>(Wc, m, k, U, sm);
+      householder_qr<T>(Wc, m, k, k, U, sm);
       if (tid == 0) sm->ival[5] = 1;  // QR taken: vectors of a degenerate cluster
       __syncthreads();
       return Wc;
@@ -721,9 +739,10 @@ __device__ void eigvals_sorted(const cx<T>* Gp, cx<T>* Af, int m, double trace, 
                                long long& cyc_trid, long long& cyc_bisect) {
   const int tid = threadIdx.x, nt = blockDim.x;
   const long long t0 = clock64();
+  const int lda = eig_ld<T>(m);
   for (int t = tid; t < m * m; t += nt) {
     const int i = t / m, j = t - i * m;
-    Af[t] = gget(Gp, i, j, m);
+    Af[i * lda + j] = gget(Gp, i, j, m);
   }
   __syncthreads();
   tridiagonalize<T>(Af, m, trace, sm);
@@ -1111,15 +1130,18 @@ __device__ void op_move_r(const ProgDesc& P, const DevOp& op, char* big, SmallSm
   cx<T>* A = sites + P.site_off[c];
   cx<T>* B = sites + P.site_off[c + 1];
   cx<T>* M = reinterpret_cast<cx<T>*>(big);
-  cx<T>* Rb = M + kMaxM * kChiLimit;
-  const int mr = 2 * dl, nc = dr;
-  for (int t = tid; t < mr * nc; t += nt) M[t] = A[t];
+  cx<T>* Rb = M + kMaxM * (kChiLimit + 1);
+  const int mr = 2 * dl, nc = dr, ld = nc | 1;  // odd row stride: conflict-free column walks
+  for (int t = tid; t < mr * nc; t += nt) {
+    const int i = t / nc, j = t - i * nc;
+    M[i * ld + j] = A[t];
+  }
   __syncthreads();
-  householder_qr<T>(M, mr, nc, Rb, sm);
+  householder_qr<T>(M, mr, nc, ld, Rb, sm);
   const int k = mr < nc ? mr : nc;
   for (int t = tid; t < mr * k; t += nt) {
     const int i = t / k, j = t - i * k;
-    A[t] = M[i * nc + j];
+    A[t] = M[i * ld + j];
   }
   cx<T>* out = reinterpret_cast<cx<T>*>(scratch);
   const int w = 2 * dr2;
@@ -1155,18 +1177,18 @@ __device__ void op_move_l(const ProgDesc& P, const DevOp& op, char* big, SmallSm
   cx<T>* A = sites + P.site_off[c];
   cx<T>* L = sites + P.site_off[c - 1];
   cx<T>* M = reinterpret_cast<cx<T>*>(big);
-  cx<T>* Rb = M + kMaxM * kChiLimit;
-  const int mr = 2 * dr, nc = dl;
+  cx<T>* Rb = M + kMaxM * (kChiLimit + 1);
+  const int mr = 2 * dr, nc = dl, ld = nc | 1;  // odd row stride: conflict-free column walks
   for (int t = tid; t < mr * nc; t += nt) {
-    const int i = t / nc, j = t - i * nc;
-    M[t] = conj(A[j * mr + i]);
+    const int j = t / mr, i = t - j * mr;  // lanes walk A's rows (contiguous loads)
+    M[i * ld + j] = conj(A[t]);
   }
   __syncthreads();
-  householder_qr<T>(M, mr, nc, Rb, sm);
+  householder_qr<T>(M, mr, nc, ld, Rb, sm);
   const int k = mr < nc ? mr : nc;
   for (int t = tid; t < k * mr; t += nt) {
     const int j = t / mr, i = t - j * mr;
-    A[t] = conj(M[i * nc + j]);
+    A[t] = conj(M[i * ld + j]);
   }
   cx<T>* out = reinterpret_cast<cx<T>*>(scratch);
   const int h = 2 * dl2;
