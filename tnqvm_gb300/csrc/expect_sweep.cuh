@@ -20,7 +20,9 @@ struct ExpLayout {
 // Transfer-matrix sweep of one Pauli string over one MPS (ITensor
 // compute_expectation_z, ITensorMPSVisitor.cpp:173-250, for any Pauli
 // letters): E <- sum_{l,s} A[l,s,:]^H (E P_s A)[l,s,:] site by site.  Step 1
-// forms Y = E A (dl x 2dr) in 4(l) x 4(r) x 2(s) register tiles and applies the
+// forms Y = E A (dl x 2dr) in 4(l) x 4(r) x 2(s) register tiles (a tile's four
+// columns are strided by the tile count, so a warp reads contiguous shared
+// memory without bank conflicts) and applies the
 // site's Pauli as the 2x2 mix X[l,s,r] = sum_s' P[s,s'] Y[l,s',r] in
 // registers; step 2 forms E' = A_mat^H X (A_mat = A as a (2dl) x dr matrix) in
 // 4 x 4 tiles.  E (ld kChiLimit) and X are work space; As receives the
@@ -56,7 +58,7 @@ __device__ void expect_sweep(const ExpTask& tk, cx<T>* E, cx<T>* As, cx<T>* X, d
 #pragma unroll
         for (int a = 0; a < 4; ++a) {
           el[a] = min(4 * bl + a, dl - 1) * LD;
-          ar[a] = min(4 * br + a, dr - 1);
+          ar[a] = min(br + a * nbr, dr - 1);  // columns strided by nbr: a warp's loads are contiguous
         }
         cx<T> y0[4][4], y1[4][4];
 #pragma unroll
@@ -85,7 +87,7 @@ __device__ void expect_sweep(const ExpTask& tk, cx<T>* E, cx<T>* As, cx<T>* X, d
         for (int a = 0; a < 4; ++a)
 #pragma unroll
           for (int b = 0; b < 4; ++b) {
-            const int l = 4 * bl + a, r = 4 * br + b;
+            const int l = 4 * bl + a, r = br + b * nbr;
             if (l < dl && r < dr) {
               cx<T> x0 = y0[a][b], x1 = y1[a][b];
               if (code == 1) {  // X
@@ -114,7 +116,7 @@ __device__ void expect_sweep(const ExpTask& tk, cx<T>* E, cx<T>* As, cx<T>* X, d
 #pragma unroll
         for (int a = 0; a < 4; ++a) {
           ri[a] = min(4 * bi + a, dr - 1);
-          rj[a] = min(4 * bj + a, dr - 1);
+          rj[a] = min(bj + a * nb, dr - 1);
         }
         cx<T> acc[4][4];
 #pragma unroll
@@ -137,7 +139,7 @@ __device__ void expect_sweep(const ExpTask& tk, cx<T>* E, cx<T>* As, cx<T>* X, d
         for (int a = 0; a < 4; ++a)
 #pragma unroll
           for (int b = 0; b < 4; ++b) {
-            const int r = 4 * bi + a, rp = 4 * bj + b;
+            const int r = 4 * bi + a, rp = bj + b * nb;
             if (r < dr && rp < dr) E[r * LD + rp] = acc[a][b];
           }
       }

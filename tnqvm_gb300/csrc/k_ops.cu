@@ -523,8 +523,9 @@ __device__ void tri_backtransform(const cx<T>* A, cx<T>* W, int m, int k, int ld
 }
 
 // C (R x Q) = A B with A(r, l), B(l, q) given by functors, in register
-// tiles of TR x TQ outputs per thread (threads take tiles with q fastest, so a
-// warp reads B contiguously and A as a broadcast).  Each output sums l = 0 ..
+// tiles of TR consecutive rows x TQ columns strided by the tile count (threads
+// take tiles with q fastest, so a warp reads B contiguously and A as a
+// broadcast).  Each output sums l = 0 ..
 // K-1 in order with fma_c, as the untiled loops do; store(r, q, value).
 template <typename T, int TR, int TQ, typename FA, typename FB, typename FS>
 __device__ __forceinline__ void tiled_product(int R, int Q, int K, FA fa, FB fb, FS store) {
@@ -535,7 +536,7 @@ __device__ __forceinline__ void tiled_product(int R, int Q, int K, FA fa, FB fb,
 #pragma unroll
     for (int a = 0; a < TR; ++a) rr[a] = min(TR * tr + a, R - 1);
 #pragma unroll
-    for (int b = 0; b < TQ; ++b) qq[b] = min(TQ * tq + b, Q - 1);
+    for (int b = 0; b < TQ; ++b) qq[b] = min(tq + b * nq, Q - 1);
     cx<T> acc[TR][TQ];
 #pragma unroll
     for (int a = 0; a < TR; ++a)
@@ -556,7 +557,7 @@ __device__ __forceinline__ void tiled_product(int R, int Q, int K, FA fa, FB fb,
     for (int a = 0; a < TR; ++a)
 #pragma unroll
       for (int b = 0; b < TQ; ++b) {
-        const int r = TR * tr + a, q = TQ * tq + b;
+        const int r = TR * tr + a, q = tq + b * nq;
         if (r < R && q < Q) store(r, q, acc[a][b]);
       }
   }
@@ -588,7 +589,7 @@ __device__ const cx<T>* orthonormalize(cx<T>* Wc, int m, int k, cx<T>* U, SmallS
 #pragma unroll
         for (int a = 0; a < 2; ++a) ca[a] = min(2 * ta + a, k - 1);
 #pragma unroll
-        for (int b = 0; b < 4; ++b) cb[b] = min(4 * tb + b, k - 1);
+        for (int b = 0; b < 4; ++b) cb[b] = min(tb + b * ntb, k - 1);  // strided: conflict-free loads
         cx<T> acc[2][4];
 #pragma unroll
         for (int a = 0; a < 2; ++a)
@@ -610,7 +611,7 @@ __device__ const cx<T>* orthonormalize(cx<T>* Wc, int m, int k, cx<T>* U, SmallS
         for (int a = 0; a < 2; ++a)
 #pragma unroll
           for (int b = 0; b < 4; ++b) {
-            const int ea = 2 * ta + a, eb = 4 * tb + b;
+            const int ea = 2 * ta + a, eb = tb + b * ntb;
             if (ea < k && eb < k) {
               cx<T> v = acc[a][b];
               if (ea == eb) v.re -= T(1);
@@ -638,7 +639,7 @@ __device__ const cx<T>* orthonormalize(cx<T>* Wc, int m, int k, cx<T>* U, SmallS
 #pragma unroll
         for (int a = 0; a < UR; ++a) ri[a] = min(UR * ti + a, m - 1) * k;
 #pragma unroll
-        for (int b = 0; b < 4; ++b) cj[b] = min(4 * tj + b, k - 1);
+        for (int b = 0; b < 4; ++b) cj[b] = min(tj + b * ntj, k - 1);  // strided: conflict-free loads
         cx<T> corr[UR][4];
 #pragma unroll
         for (int a = 0; a < UR; ++a)
@@ -659,7 +660,7 @@ __device__ const cx<T>* orthonormalize(cx<T>* Wc, int m, int k, cx<T>* U, SmallS
         for (int a = 0; a < UR; ++a)
 #pragma unroll
           for (int b = 0; b < 4; ++b) {
-            const int i = UR * ti + a, j = 4 * tj + b;
+            const int i = UR * ti + a, j = tj + b * ntj;
             if (i < m && j < k) nxt[i * k + j] = cur[i * k + j] - scl(corr[a][b], T(0.5));
           }
       }
