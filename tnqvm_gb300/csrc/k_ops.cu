@@ -120,7 +120,8 @@ struct Layout {
   // Large shared region: Gram (packed upper) [+ U for FP32], or the QR matrix + R.
   static constexpr size_t gram_bytes = sizeof(cx<T>) * (kMaxM * (kMaxM + 1) / 2);
   // U (m x m), or X staged for the Gram with a padded stride (m x (m+1))
-  static constexpr size_t u_bytes = Prec<T>::u_in_smem ? sizeof(cx<T>) * kMaxM * (kMaxM + 1) : 0;
+  // (the eigensolver's row stride is at most kMaxM + 4, see eig_ld)
+  static constexpr size_t u_bytes = Prec<T>::u_in_smem ? sizeof(cx<T>) * kMaxM * (kMaxM + 4) : 0;
   // QR of a centre move: M (<= kMaxM x kChiLimit, odd row stride <= kChiLimit + 1), then R
   static constexpr size_t qr_bytes = sizeof(cx<T>) * (kMaxM * (kChiLimit + 1) + kChiLimit * kChiLimit);
   static constexpr size_t big = (gram_bytes + u_bytes) > qr_bytes ? (gram_bytes + u_bytes) : qr_bytes;
@@ -243,13 +244,15 @@ __device__ void householder_qr(cx<T>* M, int mr, int nc, int ld, cx<T>* Rb, Smal
 // eigenvectors by one twisted factorisation each (Dhillon-Parlett), and the
 // back-transform by the stored reflectors.
 
-// Row stride of the eigensolver's m x m work matrix: odd in shared memory
-// (FP32), so column walks and the four-lanes-per-row products of the
-// tridiagonalisation are free of bank conflicts; m in global memory (FP64),
-// whose scratch holds exactly m x m.
+// Row stride of the eigensolver's m x m work matrix.  In shared memory (FP32)
+// it is the smallest value >= m that is 4 mod 16 (at most kMaxM + 4): the
+// tridiagonalisation's p = A v has four lanes per row and eight rows per
+// warp, and with that stride a half-warp's sixteen 8-byte loads fall on
+// sixteen distinct bank pairs.  In global memory (FP64) it is m, as the
+// scratch holds exactly m x m.
 template <typename T>
 __device__ __forceinline__ int eig_ld(int m) {
-  return Prec<T>::u_in_smem ? (m | 1) : m;
+  return Prec<T>::u_in_smem ? ((m + 11) & ~15) + 4 : m;
 }
 
 // A: full Hermitian m x m (row stride eig_ld(m)) in shared memory.  On return td/te hold the
