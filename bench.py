@@ -46,6 +46,27 @@ def env_int(k, d):
         return d
 
 
+def replica_seed(rank):
+    """Seed of a rank's shard of the batch: each rank simulates its own
+    circuits (replicas; no collective on the data path)."""
+    return 2024 + rank
+
+
+def max_over_ranks(ms, dist, device):
+    """The slowest rank's time: the whole job ends with it."""
+    if dist is None:
+        return ms
+    import torch
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(instances_per_rank, world, ms):
+    """Whole-job circuits/s: every rank's circuits over the slowest rank's time."""
+    return instances_per_rank * world / (ms / 1e3)
+
+
 def build_locked():
     import fcntl
     from tnqvm_gb300 import build as B
@@ -141,7 +162,7 @@ def run_reference(args):
     if rank != 0:
         return 0
     from tnqvm_gb300 import circuits
-    insts = circuits.vqe_batch(args.instances, seed=2024)
+    insts = circuits.vqe_batch(args.instances, seed=replica_seed(0))
     order = np.argsort([it["n"] * it["layers"] for it in insts])
     stride = max(1, len(order) // 64)
     pool = [insts[i] for i in order[::stride]]
@@ -187,7 +208,7 @@ def run_ours(args):
     from tnqvm_gb300 import mps as M
 
     ctx = M.Context(local)
-    insts = circuits.vqe_batch(args.instances, seed=2024 + rank, qmax=args.qmax, lmax=args.lmax)  # replica shard
+    insts = circuits.vqe_batch(args.instances, seed=replica_seed(rank), qmax=args.qmax, lmax=args.lmax)
     enc = [M.encode_circuit(it["circuit"]) for it in insts]
     progs = []
     for it, e in zip(insts, enc):
@@ -233,12 +254,10 @@ def run_ours(args):
     phase_share["orthonormalise_in_split"] = sums["cyc_orth"] / cyc_total
     phase_share["refined_splits"] = int(sums["refined"])
     phase_share["splits"] = int(sums["gate2"])
+    ms = max_over_ranks(ms, dist, "cuda")
     if dist is not None:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
         dist.barrier()
-    value = args.instances * world / (ms / 1e3)
+    value = job_throughput(args.instances, world, ms)
 
     # ---- end to end through the public API from host buffers
     e2e_times = []
@@ -250,12 +269,8 @@ def run_ours(args):
         g.launch()
         if step >= args.warmup:
             e2e_times.append(time.perf_counter() - t0)
-    e2e_ms = 1e3 * float(np.mean(e2e_times))
-    e2e_value = args.instances * world / (e2e_ms / 1e3)
-    if dist is not None:
-        t = torch.tensor([e2e_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_value = args.instances * world / (float(t.item()) / 1e3)
+    e2e_ms = max_over_ranks(1e3 * float(np.mean(e2e_times)), dist, "cuda")
+    e2e_value = job_throughput(args.instances, world, e2e_ms)
 
     extras = {}
     if rank == 0 and not args.no_extras:
