@@ -362,3 +362,34 @@ def test_engine_matches_itensor_reference_fixtures(ctx):
             vals = p.expect_pauli(c["paulis"])
             for s, v, want in zip(c["paulis"], vals, c["expect"]):
                 assert abs(v - complex(*want)) < TOL64, (c["name"], s)
+
+
+@pytest.mark.parametrize("mode", [M.TRUNC_EXATN, M.TRUNC_ITENSOR])
+def test_deuteron_h3_table_gpu(ctx, mode):
+    # tests/ExatnExpValSumReduceTester.cpp:125-240: <X0 X1> after the two exp_i_theta
+    # instructions (expanded into gates), on a subgrid of the 20 x 20 table (1e-6)
+    from tests.test_oracle_golden import deuteron_h3_circuit, reference_tables
+    tab = reference_tables()["deuteron_h3_x0x1"]["values"]
+    ang = linspace(-PI, PI, 20)
+    for i0 in range(0, 20, 3):
+        for i1 in range(0, 20, 2):
+            with run(ctx, 3, deuteron_h3_circuit(ang[i0], ang[i1]), cutoff=1e-14, mode=mode) as p:
+                v = p.expect_pauli(["ZZI"])[0]
+            assert abs(v.real - tab[20 * i0 + i1]) < 1e-6
+
+
+def test_ucc_vqe_minimum_gpu(ctx):
+    # tests/VQEModeTester.cpp:84-127: VQE minimum -1.13717 (1e-4), energies from the engine
+    import scipy.optimize
+    from tests.test_oracle_golden import UCC_TERMS, ucc_circuit
+
+    def energy(t):
+        with run(ctx, 4, ucc_circuit(float(t)), cutoff=1e-14, mode=M.TRUNC_ITENSOR) as p:
+            _, e = p.expect_pauli([s for _, s in UCC_TERMS], [c for c, _ in UCC_TERMS])
+        return e
+
+    grid = linspace(-PI, PI, 41)
+    t_best = min(grid, key=energy)
+    res = scipy.optimize.minimize_scalar(energy, bounds=(t_best - 0.2, t_best + 0.2), method="bounded",
+                                         options={"xatol": 1e-10})
+    assert abs(res.fun + 1.13717) < 1e-4

@@ -259,3 +259,101 @@ def test_oracle_matches_itensor_reference_fixtures():
         assert m.bond_dims() == c["bonds"], c["name"]
         for p, v in zip(c["paulis"], c["expect"]):
             assert abs(m.expect_pauli(p) - complex(*v)) < 1e-12, (c["name"], p)
+
+
+# ------------------------------------------------ ExatnExpValSumReduceTester
+def reference_tables():
+    import json
+    import os
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "reference_tables.json")
+    with open(path) as f:
+        return json.load(f)
+
+
+def pauli_exp_gates(paulis, theta):
+    """Gates of exp(-i theta P) for a Pauli string P (character q on qubit q):
+    basis change to Z (H for X, Rx(pi/2) for Y), a CNOT ladder over the
+    support, Rz(2 theta) on its last qubit, then the ladder and the basis
+    change undone.  This is how XACC's exp_i_theta instruction expands."""
+    sup = [q for q, c in enumerate(paulis) if c != "I"]
+    pre, post = [], []
+    for q in sup:
+        if paulis[q] == "X":
+            pre.append(("H", (q,), ()))
+            post.append(("H", (q,), ()))
+        elif paulis[q] == "Y":
+            pre.append(("Rx", (q,), (PI / 2,)))
+            post.append(("Rx", (q,), (-PI / 2,)))
+    ladder = [("CNOT", (a, b), ()) for a, b in zip(sup, sup[1:])]
+    return pre + ladder + [("Rz", (sup[-1],), (2.0 * theta,))] + ladder[::-1] + post
+
+
+def deuteron_h3_circuit(t0, t1):
+    # X(0); exp_i_theta(t0, 0.5 X0 Y1 - 0.5 Y0 X1); exp_i_theta(t1, 0.5 X0 Z1 Y2 - 0.5 X2 Z1 Y0),
+    # each exp(-i t sum_k c_k P_k) with commuting terms; then H(0), H(1) for <X0 X1>
+    circ = [("X", (0,), ())]
+    circ += pauli_exp_gates("XYI", 0.5 * t0) + pauli_exp_gates("YXI", -0.5 * t0)
+    circ += pauli_exp_gates("XZY", 0.5 * t1) + pauli_exp_gates("YZX", -0.5 * t1)
+    return circ + [("H", (0,), ()), ("H", (1,), ())]
+
+
+def test_deuteron_table_sum_reduce():
+    # tests/ExatnExpValSumReduceTester.cpp:47-80 (the same circuit as MpsGateTester's table), 1e-6
+    tab = reference_tables()["deuteron_x0x1"]["values"]
+    for i, t in enumerate(linspace(-PI, PI, 20)):
+        circ = [("X", (0,), ()), ("Ry", (1,), (t,)), ("CNOT", (1, 0), ()), ("H", (0,), ()), ("H", (1,), ())]
+        for m in both_modes(2, circ):
+            assert abs(z_expect(m, [0, 1]) - tab[i]) < 1e-6
+
+
+def test_deuteron_h3_table_dense():
+    # tests/ExatnExpValSumReduceTester.cpp:125-240: <X0 X1> on a 20 x 20 grid (1e-6), with
+    # exp_i_theta as exp(-i t G) of the summed generator
+    tab = reference_tables()["deuteron_h3_x0x1"]["values"]
+    g1 = 0.5 * (_pauli_matrix("XYI") - _pauli_matrix("YXI"))
+    g2 = 0.5 * (_pauli_matrix("XZY") - _pauli_matrix("YZX"))
+    xx = _pauli_matrix("XXI")
+    ang = linspace(-PI, PI, 20)
+    for i0, t0 in enumerate(ang):
+        for i1, t1 in enumerate(ang):
+            psi = dense.run(3, [("X", (0,), ())])
+            psi = scipy.linalg.expm(-1j * t1 * g2) @ (scipy.linalg.expm(-1j * t0 * g1) @ psi)
+            assert abs(np.real(np.vdot(psi, xx @ psi)) - tab[20 * i0 + i1]) < 1e-6
+
+
+def test_deuteron_h3_table_mps_gates():
+    # the same table through the gate expansion of exp_i_theta on the MPS oracle, both truncation modes
+    tab = reference_tables()["deuteron_h3_x0x1"]["values"]
+    ang = linspace(-PI, PI, 20)
+    for i0 in range(0, 20, 3):
+        for i1 in range(0, 20, 2):
+            for m in both_modes(3, deuteron_h3_circuit(ang[i0], ang[i1])):
+                assert abs(z_expect(m, [0, 1]) - tab[20 * i0 + i1]) < 1e-6
+
+
+UCC_TERMS = [(0.174073, "IIZZ"), (0.1202, "IZIZ"), (0.165607, "IZZI"), (0.165607, "ZIIZ"), (0.1202, "ZIZI"),
+             (-0.0454063, "YYXX"), (-0.220041, "IIIZ"), (-0.106477, "IIII"), (0.17028, "ZIII"),
+             (-0.220041, "IIZI"), (0.17028, "IZII"), (-0.0454063, "XXYY"), (0.0454063, "XYYX"),
+             (0.168336, "ZZII"), (0.0454063, "YXXY")]  # tests/VQEModeTester.cpp:107-112
+
+
+def ucc_circuit(t0):
+    # tests/VQEModeTester.cpp:84-103
+    c = [("X", (0,), ()), ("X", (1,), ()), ("Rx", (0,), (1.5707,)), ("H", (1,), ()), ("H", (2,), ()),
+         ("H", (3,), ()), ("CNOT", (0, 1), ()), ("CNOT", (1, 2), ()), ("CNOT", (2, 3), ()), ("Rz", (3,), (t0,)),
+         ("CNOT", (2, 3), ()), ("CNOT", (1, 2), ()), ("CNOT", (0, 1), ()), ("Rx", (0,), (-1.5707,)),
+         ("H", (1,), ()), ("H", (2,), ()), ("H", (3,), ())]
+    return c
+
+
+def test_ucc_vqe_minimum():
+    # tests/VQEModeTester.cpp:84-127: VQE minimum -1.13717 (1e-4), here by a bounded scalar search
+    def energy(t):
+        m = mps.run(4, ucc_circuit(float(t)), mode="itensor", cutoff=1e-14)
+        return sum(c * m.expect_pauli(s).real for c, s in UCC_TERMS)
+
+    grid = linspace(-PI, PI, 41)
+    t_best = min(grid, key=energy)
+    res = scipy.optimize.minimize_scalar(energy, bounds=(t_best - 0.2, t_best + 0.2), method="bounded",
+                                         options={"xatol": 1e-10})
+    assert abs(res.fun + 1.13717) < 1e-4
