@@ -357,3 +357,21 @@ def test_ucc_vqe_minimum():
     res = scipy.optimize.minimize_scalar(energy, bounds=(t_best - 0.2, t_best + 0.2), method="bounded",
                                          options={"xatol": 1e-10})
     assert abs(res.fun + 1.13717) < 1e-4
+
+
+def test_deutsch_jozsa_16_routed():
+    # visitors/exatn-mps/tests/BigCircuitTester.cpp:41-145: 16-bit Deutsch-Jozsa with a balanced
+    # parity oracle (CNOTs from every input qubit to the ancilla q16, routed over up to 16 sites);
+    # the inputs then read 1...1 with certainty
+    n = 17
+    evens = [("X", (q,), ()) for q in range(0, 16, 2)]
+    circ = [("X", (16,), ())] + [("H", (q,), ()) for q in range(17)] + evens
+    circ += [("CNOT", (q, 16), ()) for q in range(16)] + evens + [("H", (q,), ()) for q in range(16)]
+    routed = routing.route(circ)
+    assert all(len(q) == 1 or abs(q[0] - q[1]) == 1 for _, q, _ in routed)
+    psi = dense.run(n, routed)
+    for m in both_modes(n, circ, chi_max=64):
+        for q in range(16):
+            assert abs(z_expect(m, [q]) + 1.0) < 1e-10
+    p = dense.probabilities(psi, list(range(16)))
+    assert abs(p[(1 << 16) - 1] - 1.0) < 1e-10
