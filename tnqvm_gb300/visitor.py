@@ -14,7 +14,9 @@ Options (``setOptions``), as in ``TNQVM::updateConfiguration``
 (``ExaTnMpsVisitor.cpp:257-271``): ``svd-cutoff`` (default DBL_MIN),
 ``max-bond-dim`` (default: the build's limit), ``shots``, ``seed``, plus
 ``truncation-mode`` (``exatn`` | ``itensor``), ``precision`` (``fp64`` |
-``fp32``), ``renormalize`` and ``per-gate`` (one launch per gate).
+``fp32``), ``renormalize``, ``per-gate`` (one launch per gate), and for bond
+caps above 64 ``gemm-autotune`` (0 static, 1 tune, 2 table) and
+``gemm-tune-cache`` (a saved tuning table, used without trial launches).
 """
 from collections import Counter
 
@@ -120,6 +122,12 @@ class GpuMpsVisitor:
                 (M.FLAG_PER_GATE if o.get("per-gate", False) else 0)
         cutoff = float(o["svd-cutoff"]) if "svd-cutoff" in o else -1.0
         chi = int(o["max-bond-dim"]) if "max-bond-dim" in o else 0
+        # GEMM kernel choice of the wide path (no counterpart in the reference)
+        if "gemm-tune-cache" in o:
+            M.autotune_load(o["gemm-tune-cache"])
+            M.autotune_set_mode(2)
+        if "gemm-autotune" in o:
+            M.autotune_set_mode(int(o["gemm-autotune"]))
         if self.prog is not None:
             self.prog.close()
         self.buffer = buffer

@@ -65,6 +65,15 @@ void GpuMpsVisitor::initialize(std::shared_ptr<AcceleratorBuffer> in_buffer, int
   int flags = 0;
   if (options.keyExists<bool>("renormalize") && options.get<bool>("renormalize")) flags |= MPS_FLAG_RENORM;
   if (options.keyExists<bool>("per-gate") && options.get<bool>("per-gate")) flags |= MPS_FLAG_PER_GATE;
+  // GEMM kernel choice of the wide path (bond caps above 64); no counterpart in
+  // the reference: "gemm-tune-cache" loads a saved table and uses it without
+  // trial launches, "gemm-autotune" sets the mode (0 static, 1 tune, 2 table)
+  if (options.keyExists<std::string>("gemm-tune-cache")) {
+    check(mps_autotune_load(options.get<std::string>("gemm-tune-cache").c_str()), "gemm-tune-cache");
+    check(mps_autotune_set_mode(2), "gemm-tune-cache");
+  }
+  if (options.keyExists<int>("gemm-autotune"))
+    check(mps_autotune_set_mode(options.get<int>("gemm-autotune")), "gemm-autotune");
   buffer = std::move(in_buffer);
   shots_ = nbShots;
   measured_.clear();
