@@ -101,3 +101,51 @@ def test_autotune_host_calls(tmp_path):
     finally:
         M.autotune_clear()
         M.autotune_set_mode(old)
+
+
+_NULL_SWEEP = r'''
+import ctypes, sys
+sys.path.insert(0, sys.argv[1])
+from tnqvm_gb300 import mps as M
+lib = M.load_library()
+for name, res, argtypes in M.SIGNATURES:
+    args = []
+    for a in argtypes:
+        if a in (ctypes.c_int, ctypes.c_int32, ctypes.c_int64, ctypes.c_uint64, ctypes.c_size_t):
+            args.append(0)
+        elif a is ctypes.c_double:
+            args.append(0.0)
+        else:
+            args.append(None)
+    rc = getattr(lib, name)(*args)
+    print(name, rc if res is ctypes.c_int else "-", flush=True)
+'''
+
+# entry points for which NULL / zero arguments are a valid no-op (as free(NULL))
+# or a valid setting
+_NULL_OK = {"mps_ctx_destroy", "mps_program_destroy", "mps_graph_destroy", "mps_serve_stop",
+            "mps_autotune_set_mode", "mps_autotune_clear"}
+
+
+def test_null_arguments_are_errors_not_crashes():
+    """Every entry point called with NULL handles and zero sizes returns a
+    status (MPS_ERR_ARG, or MPS_OK where that is a valid no-op) without
+    touching memory; run in a child process so a crash cannot take pytest
+    down."""
+    import subprocess
+    import sys
+    r = subprocess.run([sys.executable, "-c", _NULL_SWEEP, ROOT], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout[-500:] + r.stderr[-500:]
+    from tnqvm_gb300 import mps as M
+    seen = {}
+    for line in r.stdout.strip().splitlines():
+        name, rc = line.split()
+        seen[name] = rc
+    assert set(seen) == {s[0] for s in M.SIGNATURES}
+    for name, rc in seen.items():
+        if rc == "-":
+            continue
+        if name in _NULL_OK:
+            assert rc == "0", name
+        else:
+            assert rc == str(M.ERR_ARG), (name, rc)
