@@ -375,3 +375,21 @@ def test_deutsch_jozsa_16_routed():
             assert abs(z_expect(m, [q]) + 1.0) < 1e-10
     p = dense.probabilities(psi, list(range(16)))
     assert abs(p[(1 << 16) - 1] - 1.0) < 1e-10
+
+
+def test_sampler_distribution():
+    # visitors/exatn-mps/tests/NumericalTester.cpp: a 5-qubit random circuit, 100000 shots, every
+    # sampled bit string's frequency within 0.01 of its probability; plus a chi-square test
+    from scipy import stats
+    from tnqvm_gb300 import circuits
+    n = 5
+    psi = dense.run(n, circuits.brickwall(n, 15, seed=31))
+    meas = list(range(n))
+    p = dense.probabilities(psi, meas)
+    bits = dense.sample(psi, meas, 100000, np.random.default_rng(5))
+    keys = (bits.astype(np.int64) << np.arange(n)).sum(axis=1)
+    counts = np.bincount(keys, minlength=1 << n)
+    assert np.max(np.abs(counts / 100000 - p)) < 0.01
+    mask = p * 100000 >= 5
+    chi2 = (((counts - 100000 * p) ** 2) / np.where(mask, 100000 * p, 1.0))[mask].sum()
+    assert stats.chi2.sf(chi2, mask.sum() - 1) > 1e-4
