@@ -393,3 +393,23 @@ def test_ucc_vqe_minimum_gpu(ctx):
     res = scipy.optimize.minimize_scalar(energy, bounds=(t_best - 0.2, t_best + 0.2), method="bounded",
                                          options={"xatol": 1e-10})
     assert abs(res.fun + 1.13717) < 1e-4
+
+
+def test_admission_budget():
+    """Admission by projected HBM footprint (sum of chi_l * 2 * chi_r * bytes):
+    a context whose budget holds two programs refuses a third with
+    MPS_ERR_OOM and admits it again once one is destroyed."""
+    one = M.footprint_bytes(10, 16, M.PREC_FP64)
+    with M.Context(0, hbm_budget_bytes=2 * one + one // 2) as c2:
+        a = M.Program(c2, 10, 16)
+        b = M.Program(c2, 10, 16)
+        assert c2.bytes_resident == 2 * one
+        with pytest.raises(M.MpsError) as e:
+            M.Program(c2, 10, 16)
+        assert e.value.code == M.ERR_OOM
+        a.close()
+        d = M.Program(c2, 10, 16)
+        assert c2.bytes_resident == 2 * one
+        b.close()
+        d.close()
+        assert c2.bytes_resident == 0
