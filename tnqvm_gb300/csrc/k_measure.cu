@@ -15,6 +15,7 @@
 //               with every index closed).
 #include "expect_sweep.cuh"
 #include "mps_common.cuh"
+#include "philox.cuh"
 
 namespace gbmps {
 
@@ -66,24 +67,8 @@ __global__ void __launch_bounds__(256) k_right_env(EnvTask tk, char* scratch) {
   }
 }
 
-// Philox4x32-10 (Random123 constants).
-__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k) {
-#pragma unroll
-  for (int r = 0; r < 10; ++r) {
-    const uint32_t hi0 = __umulhi(0xD2511F53u, c.x), lo0 = 0xD2511F53u * c.x;
-    const uint32_t hi1 = __umulhi(0xCD9E8D57u, c.z), lo1 = 0xCD9E8D57u * c.z;
-    c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
-    k.x += 0x9E3779B9u;
-    k.y += 0xBB67AE85u;
-  }
-  return c;
-}
-
 __device__ __forceinline__ double uniform01(uint64_t seed, uint32_t shot, uint32_t site) {
-  const uint4 r = philox4x32_10(make_uint4(shot, site, 0x4d505321u, 0u),
-                                make_uint2((uint32_t)seed, (uint32_t)(seed >> 32)));
-  const uint64_t v = ((uint64_t)r.x << 32) | r.y;
-  return (double)(v >> 11) * (1.0 / 9007199254740992.0);
+  return philox_uniform(seed, shot, site, 0x4d505321u);
 }
 
 

@@ -24,6 +24,7 @@
 #include "../../include/gb300mps.h"
 #include "engine_internal.hpp"
 #include "keep.cuh"
+#include "philox.cuh"
 #include "wide.hpp"
 
 namespace gbmps {
@@ -202,20 +203,9 @@ __global__ void k_store_scalar(const cx<T>* E, double* out) {
   out[1] = (double)E[0].im;
 }
 
-// Philox4x32-10 (Salmon et al., SC'11) uniform in [0, 1) for (shot, site).
+// Philox4x32-10 uniform in [0, 1) for (shot, site), its own stream tag.
 __device__ __forceinline__ double wide_uniform(uint64_t seed, uint32_t shot, uint32_t site) {
-  uint4 c = make_uint4(shot, site, 0x57494445u, 0u);
-  uint2 k = make_uint2((uint32_t)seed, (uint32_t)(seed >> 32));
-#pragma unroll
-  for (int r = 0; r < 10; ++r) {
-    const uint32_t hi0 = __umulhi(0xD2511F53u, c.x), lo0 = 0xD2511F53u * c.x;
-    const uint32_t hi1 = __umulhi(0xCD9E8D57u, c.z), lo1 = 0xCD9E8D57u * c.z;
-    c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
-    k.x += 0x9E3779B9u;
-    k.y += 0xBB67AE85u;
-  }
-  const uint64_t v = ((uint64_t)c.x << 32) | c.y;
-  return (double)(v >> 11) * (1.0 / 9007199254740992.0);
+  return philox_uniform(seed, shot, site, 0x57494445u);
 }
 
 // One site of shot sampling: U (S x 2dr, cols (s, r)) = V A, Q = U R_{i+1}
