@@ -79,6 +79,23 @@ def test_truncated_fp64_vs_oracle(ctx, mode, omode, chi):
         assert abs(p.truncation_fidelity() - ref.fidelity) < 1e-9
 
 
+@pytest.mark.parametrize("mode,omode", [(M.TRUNC_ITENSOR, "itensor"), (M.TRUNC_EXATN, "exatn")])
+@pytest.mark.parametrize("chi", [4, 8])
+def test_renormalised_fp64_vs_oracle(ctx, mode, omode, chi):
+    """MPS_FLAG_RENORM: each truncated split rescaled to its pre-truncation
+    weight, against the oracle with the same rule (1e-9)."""
+    n = 10
+    circ = circuits.brickwall(n, 8, seed=5)
+    ref = omps.run(n, routing.route(circ), mode=omode, chi_max=chi, cutoff=1e-12, renorm=True)
+    paulis = ["XYZIZXYIZX", "ZZIIIIIIII", "IIIIZZIIII", "YIIIIIIIIY", "IIIIIIIIII"]
+    with run(ctx, n, circ, chi, 1e-12, mode, M.PREC_FP64, M.FLAG_RENORM) as p:
+        assert p.bond_dims() == ref.bond_dims()
+        vals = p.expect_pauli(paulis)
+        for s, v in zip(paulis, vals):
+            assert abs(v - ref.expect_pauli(s)) < 1e-9, s
+        assert abs(p.truncation_fidelity() - ref.fidelity) < 1e-9
+
+
 def test_hea_truncated_fp32_vs_fp64_oracle(ctx):
     """The complex64 engine with canonical truncation against the complex128
     oracle at the same cap: |dE| <= 1e-6 on a 50-term Hamiltonian."""

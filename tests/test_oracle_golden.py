@@ -393,3 +393,24 @@ def test_sampler_distribution():
     mask = p * 100000 >= 5
     chi2 = (((counts - 100000 * p) ** 2) / np.where(mask, 100000 * p, 1.0))[mask].sum()
     assert stats.chi2.sf(chi2, mask.sum() - 1) > 1e-4
+
+
+@pytest.mark.parametrize("mode", ["exatn", "itensor"])
+def test_renormalisation_is_a_global_scale(mode):
+    # the renormalise flag rescales each truncated split to its pre-truncation weight: the state
+    # changes only by a global factor (canonical itensor form then keeps norm 1)
+    from tnqvm_gb300 import circuits
+    n = 10
+    circ = routing.route(circuits.brickwall(n, 8, seed=13))
+    cut = 1e-3 if mode == "exatn" else 1e-12
+    plain = mps.run(n, circ, mode=mode, chi_max=6, cutoff=cut)
+    ren = mps.run(n, circ, mode=mode, chi_max=6, cutoff=cut, renorm=True)
+    assert plain.bond_dims() == ren.bond_dims() and max(plain.bond_dims()) == 6
+    assert plain.fidelity < 0.99
+    if mode == "itensor":
+        assert abs(ren.norm2() - 1.0) < 1e-12
+        assert abs(plain.norm2() - plain.fidelity) < 1e-10
+    for s in ["Z" * n, "XY" + "I" * (n - 2), "I" * 4 + "ZXZ" + "I" * 3]:
+        a = plain.expect_pauli(s) / plain.norm2()
+        b = ren.expect_pauli(s) / ren.norm2()
+        assert abs(a - b) < 1e-12, s
