@@ -200,12 +200,13 @@ int mps_serve_stop(mps_ctx* ctx);
 
 /* Allocation-free two-site update.  No counterpart in the reference: TNQVM's
  * visitors always allocate through ExaTN/ITensor.  It exists for callers that
- * cannot call cudaMalloc: code recording into a CUDA graph, processes whose
- * device memory belongs to another allocator (a framework's memory pool), and
- * latency-critical loops where an allocation's implicit synchronisation is not
- * allowed.  It allocates nothing (no cudaMalloc/cudaFree, no allocating
- * library call); its scratch is one file-scope device array of 256 B + 512 KiB
- * that every GPU which loads this library holds until the process exits.
+ * cannot call cudaMalloc: a plugin inside a host application whose device
+ * memory belongs to that application's own pool allocator (reserved up front,
+ * so a cudaMalloc fails or is forbidden), or a process under a fixed
+ * device-memory cap.  It allocates nothing (no cudaMalloc/cudaFree, no
+ * allocating library call); its scratch is one file-scope device array of
+ * 256 B + 512 KiB that every GPU which loads this library holds until the
+ * process exits.
  *
  * The caller owns all inputs and outputs, in device memory:
  *   sites      element buffer (complex128 or complex64 by precision) holding
@@ -218,12 +219,14 @@ int mps_serve_stop(mps_ctx* ctx);
  * 4x4 gate (row = 2*phys(lo) + phys(hi)) and the stream to run on.
  * exatn semantics split sqrt(S) onto both sites; itensor semantics leave the
  * lo site left-isometric (the caller keeps the orthogonality centre on the
- * pair).  Bonds above 64 are rejected with MPS_ERR_UNSUPPORTED.  The first
- * call on a device looks up the array's device address and sets the kernel's
- * shared-memory limit, so make that first call before any stream capture.
- * Every call shares the one array and the call waits for its kernel, so two
- * calls that overlap on the GPU (e.g. issued from two host threads on two
- * streams) race on it. */
+ * pair).  Bonds above 64 are rejected with MPS_ERR_UNSUPPORTED, and a
+ * hi_offset below 2*dl*max(dm, min(2*dl, 2*dr, chi_max)) (the hi site would
+ * overlap the lo site) with MPS_ERR_ARG.  The first call on a device looks up
+ * the array's device address and sets the kernel's shared-memory limit, so
+ * make that first call before any stream capture.  Each call waits for its
+ * kernel and reads the error word back, so it synchronises the stream.
+ * Every call shares the one array, so two calls that overlap on the GPU (e.g.
+ * issued from two host threads on two streams) race on it. */
 int mps_gate2_apply_noalloc(int precision, int trunc_mode, int chi_max, double cutoff, void* sites,
                             int64_t hi_offset, int* d_bonds, const int* bonds, const double gate[32],
                             void* cuda_stream);

@@ -10,7 +10,9 @@ import os
 import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = "/root/reference"
+# the reference tree: TNQVM_REFERENCE_ROOT, else a "reference" folder beside the repository
+REF = os.environ.get("TNQVM_REFERENCE_ROOT") or os.path.join(os.path.dirname(os.path.dirname(os.path.dirname(HERE))),
+                                                             "reference")
 BINARY = os.path.join(os.path.dirname(HERE), "_ref", "itensor_driver")
 
 

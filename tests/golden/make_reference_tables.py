@@ -1,9 +1,11 @@
 """Extract the hard-coded expectation tables of the reference's
 ExatnExpValSumReduceTester (tnqvm/tests/ExatnExpValSumReduceTester.cpp) into
 ``reference_tables.json``, so the tests can pin the oracle and the engine to
-them without the reference tree.  Run here, where the reference tree exists:
+them without the reference tree.  Run where the reference tree exists, giving
+its root as the argument (or in TNQVM_REFERENCE_ROOT; else a "reference"
+folder beside the repository is used):
 
-    python tests/golden/make_reference_tables.py
+    python tests/golden/make_reference_tables.py <reference root>
 """
 import json
 import os
@@ -11,8 +13,9 @@ import re
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-SRC = os.path.join(sys.argv[1] if len(sys.argv) > 1 else "/root/reference",
-                   "tnqvm", "tests", "ExatnExpValSumReduceTester.cpp")
+REF = (sys.argv[1] if len(sys.argv) > 1 else os.environ.get("TNQVM_REFERENCE_ROOT")
+       or os.path.join(os.path.dirname(os.path.dirname(os.path.dirname(HERE))), "reference"))
+SRC = os.path.join(REF, "tnqvm", "tests", "ExatnExpValSumReduceTester.cpp")
 
 
 def main():

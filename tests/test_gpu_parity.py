@@ -15,6 +15,13 @@ pytestmark = pytest.mark.gpu
 PI = np.pi
 TOL64 = 1e-10
 TOL32 = 2e-5
+# Truncated complex128 runs against the oracle's LAPACK SVD.  The sums the
+# split needs (Gram, eigenvalues) round to ~1e-16 of the largest singular
+# value; with the singular values of the sqrt(S) split taken from |w_j^H X|
+# the engine agrees to ~4e-14 (chi 4..16, both semantics, with and without
+# renormalisation).  With sqrt(lambda) of the Gram eigenvalues instead, the
+# exatn runs were off by up to 1.1e-9.
+TOL_TRUNC64 = 1e-12
 
 
 def run(ctx, n, circ, chi=0, cutoff=-1.0, mode=M.TRUNC_EXATN, prec=M.PREC_FP64, flags=0):
@@ -75,15 +82,17 @@ def test_truncated_fp64_vs_oracle(ctx, mode, omode, chi):
         assert p.bond_dims() == ref.bond_dims()
         vals = p.expect_pauli(paulis)
         for s, v in zip(paulis, vals):
-            assert abs(v - ref.expect_pauli(s)) < 1e-9, s
-        assert abs(p.truncation_fidelity() - ref.fidelity) < 1e-9
+            assert abs(v - ref.expect_pauli(s)) < TOL_TRUNC64, s
+        assert abs(p.truncation_fidelity() - ref.fidelity) < TOL_TRUNC64
 
 
 @pytest.mark.parametrize("mode,omode", [(M.TRUNC_ITENSOR, "itensor"), (M.TRUNC_EXATN, "exatn")])
 @pytest.mark.parametrize("chi", [4, 8])
 def test_renormalised_fp64_vs_oracle(ctx, mode, omode, chi):
     """MPS_FLAG_RENORM: each truncated split rescaled to its pre-truncation
-    weight, against the oracle with the same rule (1e-9)."""
+    weight, against the oracle with the same rule.  In exatn semantics the
+    state is not canonical and its norm grows with every rescale (<psi|psi> =
+    2.9 at chi 4); the values are compared unnormalised at TOL_TRUNC64."""
     n = 10
     circ = circuits.brickwall(n, 8, seed=5)
     ref = omps.run(n, routing.route(circ), mode=omode, chi_max=chi, cutoff=1e-12, renorm=True)
@@ -92,8 +101,8 @@ def test_renormalised_fp64_vs_oracle(ctx, mode, omode, chi):
         assert p.bond_dims() == ref.bond_dims()
         vals = p.expect_pauli(paulis)
         for s, v in zip(paulis, vals):
-            assert abs(v - ref.expect_pauli(s)) < 1e-9, s
-        assert abs(p.truncation_fidelity() - ref.fidelity) < 1e-9
+            assert abs(v - ref.expect_pauli(s)) < TOL_TRUNC64, s
+        assert abs(p.truncation_fidelity() - ref.fidelity) < TOL_TRUNC64
 
 
 def test_hea_truncated_fp32_vs_fp64_oracle(ctx):
@@ -363,6 +372,10 @@ def test_vqe_mode_observed_circuits(ctx):
            ("Measure", (2,), ())]
     e = v.getExpectationValueZ(obs)
     assert abs(e - dense.expect_pauli(psi, n, "XZYI").real) < TOL64
+    # Rx(t)^H Z Rx(t) = cos t Z + sin t Y: Rx(-pi/2) measures -Y
+    obs = [("Rx", (1,), (-PI / 2,)), ("Rx", (3,), (PI / 2,)), ("Measure", (1,), ()), ("Measure", (3,), ())]
+    e = v.getExpectationValueZ(obs)
+    assert abs(e + dense.expect_pauli(psi, n, "IYIY").real) < TOL64
 
 
 def test_engine_matches_itensor_reference_fixtures(ctx):

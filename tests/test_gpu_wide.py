@@ -2,8 +2,8 @@
 tensor-core complex GEMMs, the cooperative eigensolver and QR, centre moves,
 GEMM-sweep expectations and sampling, called through the C ABI and checked
 against the CPU oracle.  Tolerances: 1e-10 for complex128 runs against the
-complex128 oracle (1e-8 for truncated exatn-mode runs, whose non-canonical
-Gram matrices square a larger condition number); 4e-6 relative (Frobenius)
+complex128 oracle (1e-12 for truncated runs, whose sums round to ~1e-16 of
+the largest singular value of each split); 4e-6 relative (Frobenius)
 for one complex64 3xTF32 GEMM with K up to 1000; 1e-4 on amplitudes and 2e-5
 on expectation values for complex64 circuits."""
 import numpy as np
@@ -80,7 +80,7 @@ def test_wide_truncated_fp64_vs_oracle(ctx, mode, omode):
     with run(ctx, n, circ, 80, 1e-12, mode, M.PREC_FP64) as p:
         assert p.bond_dims() == ref.bond_dims()
         vals = p.expect_pauli(paulis)
-        tol = 1e-9 if mode == M.TRUNC_ITENSOR else 1e-8
+        tol = 1e-12
         for s, v in zip(paulis, vals):
             assert abs(v - ref.expect_pauli(s)) < tol, s
         assert abs(p.truncation_fidelity() - ref.fidelity) < tol

@@ -17,19 +17,21 @@ def test_plugin_compiles_and_links():
     assert path.endswith("visitor_demo")
 
 
-def _script(n, shots, circ, opts=()):
+def _script(n, shots, circ, opts=(), obs=()):
     lines = ["%d %d" % (n, shots)]
     for k, v in opts:
         lines.append("opt %s %s" % (k, v))
-    for name, qs, ps in circ:
-        lines.append("%s %d %s %d %s" % (name, len(qs), " ".join(map(str, qs)), len(ps),
-                                         " ".join("%.17g" % p for p in ps)))
+    for prefix, gates in (("", circ), ("obs ", obs)):
+        for name, qs, ps in gates:
+            lines.append("%s%s %d %s %d %s" % (prefix, name, len(qs), " ".join(map(str, qs)), len(ps),
+                                               " ".join("%.17g" % p for p in ps)))
     return "\n".join(lines) + "\n"
 
 
-def _run(n, shots, circ, opts=()):
+def _run(n, shots, circ, opts=(), obs=()):
     exe = B.build_visitor_demo()
-    r = subprocess.run([exe], input=_script(n, shots, circ, opts), capture_output=True, text=True, timeout=300)
+    r = subprocess.run([exe], input=_script(n, shots, circ, opts, obs), capture_output=True, text=True,
+                       timeout=300)
     assert r.returncode == 0, r.stderr
     return json.loads(r.stdout)
 
@@ -67,3 +69,18 @@ def test_plugin_wide_bond_cap():
     out = _run(n, 0, circ, [("max-bond-dim", 128), ("svd-cutoff", 1e-14)])
     assert abs(out["norm"] - 1.0) < 1e-10
     assert abs(out["exp-val-z"] - dense.expect_z_parity(psi, [1, 6, 12])) < 1e-10
+
+
+@pytest.mark.gpu
+def test_plugin_vqe_basis_signs():
+    """VQE mode through the plugin (TNQVM.cpp:82-89): measuring Z after H is
+    <X>, after Rx(pi/2) <Y> and after Rx(-pi/2) -<Y> (Rx(t)^H Z Rx(t) = cos t Z
+    + sin t Y)."""
+    n = 3
+    circ = circuits.hea(n, 2, seed=8)
+    psi = dense.run(n, circ)
+    for t, sign in ((np.pi / 2, 1.0), (-np.pi / 2, -1.0)):
+        obs = [("H", (0,), ()), ("Rx", (2,), (t,)), ("Measure", (0,), ()), ("Measure", (2,), ())]
+        out = _run(n, 0, circ, [("truncation-mode", "itensor")], obs)
+        want = sign * dense.expect_pauli(psi, n, "XIY").real
+        assert abs(out["vqe-exp-val"] - want) < 1e-10, (t, out["vqe-exp-val"], want)

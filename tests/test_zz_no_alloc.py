@@ -1,12 +1,14 @@
 """The allocation-free two-site update (mps_gate2_apply_noalloc), called
 through the C ABI, against the regular entry points.
 
-It serves callers that cannot call cudaMalloc (stream capture, a foreign
-allocator owning device memory, latency-critical loops): the test allocates
-the input/output tensors itself with torch and hands their device pointers
-over; the entry point must produce what the allocating program path
-produces, on two calls in a row, within this suite's tolerances (1e-10 for
-complex128, 2e-5 for complex64).  Kept in its own file so that it runs last.
+It serves callers that cannot call cudaMalloc: a plugin inside a host
+application whose device memory belongs to that application's own pool
+allocator, or a process under a fixed device-memory cap.  Like such a
+caller, the test owns the input/output tensors (allocated with torch) and
+hands their device pointers over; the entry point must produce what the
+allocating program path produces, on two calls in a row, within this
+suite's tolerances (1e-10 for complex128, 2e-5 for complex64).  Kept in its
+own file so that it runs last.
 """
 import ctypes
 
@@ -107,3 +109,9 @@ def test_noalloc_rejects_bonds_beyond_limit():
     rc = _call(M.PREC_FP64, M.TRUNC_EXATN, 0, sites, 2, d_bonds, [65, 1, 1], np.eye(4))
     assert rc == M.ERR_UNSUPPORTED
     assert b"64" in M._lib.mps_last_error()
+    # a hi site that would overlap the lo site's input or output is refused
+    sites = torch.zeros(64, dtype=torch.complex128, device="cuda")
+    for bonds, hi in (([2, 2, 2], 4), ([2, 4, 2], 12), ([1, 1, 1], -1)):
+        rc = _call(M.PREC_FP64, M.TRUNC_EXATN, 0, sites, hi, d_bonds, bonds, np.eye(4))
+        assert rc == M.ERR_ARG, (bonds, hi)
+        assert b"hi_offset" in M._lib.mps_last_error()

@@ -18,6 +18,7 @@
 // by singular values).
 #include <math.h>
 
+#include <algorithm>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -823,6 +824,10 @@ __device__ void op_gate2(const ProgDesc& P, const DevOp& op, char* big, SmallSme
       cx<T> acc = mk<T>(0, 0);
 #pragma unroll
       for (int col = 0; col < 4; ++col) fma_c(acc, sm->g[row * 4 + col], t[col]);
+      // exatn semantics: entries of modulus below 1e-100 are set to zero
+      // before the split (stabilizeTensorBody, ExaTnMpsVisitor.cpp:141-161);
+      // no complex64 value is that small, so only complex128 checks
+      if (sizeof(T) == 8 && P.mode == TRUNC_EXATN && (double)abs2(acc) < 1e-200) acc = mk<T>(0, 0);
       Th[(l * 2 + (row >> 1)) * Cc + (row & 1) * dr + r] = acc;
     }
   }
@@ -1083,17 +1088,50 @@ __device__ void op_gate2(const ProgDesc& P, const DevOp& op, char* big, SmallSme
   cyc_vec += c_orth - c_vec;
   cyc_orth += clock64() - c_orth;
   // other side: Z = W_k^H X (k x nn)
+  const bool sqrt_split = op.orient == ORIENT_SQRT;
   {
     constexpr int TR = sizeof(T) == 4 ? 4 : 2;
     tiled_product<T, TR, 4>(
         k, nn, m, [&](int j, int i) { return conj(W[i * k + j]); }, [&](int i, int c) { return X(i, c); },
         [&](int j, int c, cx<T> v) {
-          const cx<T> acc = scl(v, sm->oth[j]);
+          const cx<T> acc = sqrt_split ? v : scl(v, sm->oth[j]);
           if (!tr)
             B[j * Cc + c] = acc;  // hi site (k, 2, dr)
           else
             A[c * k + j] = acc;   // lo site (dl, 2, k)
         });
+  }
+  if (sqrt_split) {
+    // sqrt(S) on both sides needs each kept singular value to its own
+    // relative accuracy.  sqrt(lambda) of the Gram eigenvalue carries an
+    // absolute error ~eps * lambda_max, i.e. ~eps * (sigma_max / sigma)^2
+    // relative, and that error moves the gauge of both sites and with it
+    // every later truncation.  The row norm |w_j^H X| is accurate to ~eps *
+    // sigma_max / sigma, as ITensor's singular values from the QR of M^H U
+    // are (SVDRefImpl, tensor/algs.cc:541-548).  Columns whose eigenvalue
+    // counts as zero stay zero on both sides.
+    __syncthreads();
+    const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+    for (int j = warp; j < k; j += nw) {
+      double s2 = 0.0;
+      for (int c = lane; c < nn; c += 32) s2 += (double)abs2(!tr ? B[j * Cc + c] : A[c * k + j]);
+      for (int o = 16; o > 0; o >>= 1) s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+      if (lane == 0) {
+        const double h = sm->lk[j] > 0.0 ? sqrt(sqrt(s2)) : 0.0;
+        sm->iso[j] = T(h);
+        sm->oth[j] = T(h > 0.0 ? rn / h : 0.0);
+      }
+    }
+    __syncthreads();
+    for (int t = tid; t < k * nn; t += nt) {
+      if (!tr) {
+        const int j = t / nn;
+        B[t] = scl(B[t], sm->oth[j]);  // rows j of the hi site, (k, 2, dr) = k x nn
+      } else {
+        const int j = t - (t / k) * k;
+        A[t] = scl(A[t], sm->oth[j]);  // lo site (dl, 2, k) = nn x k
+      }
+    }
   }
   // isometric side: W_k
   for (int t = tid; t < m * k; t += nt) {
@@ -1310,27 +1348,34 @@ cudaError_t launch_ops(int prec, const ProgDesc* d_progs, int n_progs, int grid,
 }
 
 // ------------------------------------------------- allocation-free variant
-// Some callers cannot allocate device memory: code running inside a CUDA
-// stream capture that must not create allocations, hosts whose device memory
-// is owned by another allocator (a framework pool), or latency-critical
-// loops where cudaMalloc/cudaFree and their implicit synchronisation are
-// forbidden.  For them, mps_gate2_apply_noalloc runs one fused two-site
-// update with all of its scratch (theta, the FP64 eigenvector matrix, the
-// site offsets, statistics and the error word) in the file-scope array
-// below, which every GPU that loads this library holds until process exit.
+// Some callers cannot allocate device memory: a plugin loaded into a host
+// application whose device memory belongs to that application's own pool
+// allocator (every byte reserved up front, cudaMalloc forbidden or failing),
+// or a process running under a fixed device-memory cap.  For them,
+// mps_gate2_apply_noalloc runs one fused two-site update with all of its
+// scratch (theta, the FP64 eigenvector matrix, the two site offsets,
+// statistics and the error word) in the file-scope array below, which every
+// GPU that loads this library holds until process exit.
 constexpr size_t kNoAllocHeader = 256;  // two site offsets, stats, error word
 constexpr size_t kNoAllocScratch = Layout<double>::scratch;  // largest per-CTA scratch (FP64)
 constexpr size_t kNoAllocBytes = kNoAllocHeader + kNoAllocScratch;  // 256 B + 512 KiB
 static __device__ __align__(256) char g_noalloc_scratch[kNoAllocBytes];
 static_assert(64 + sizeof(double) * ST_COUNT <= 192, "stats must end before the error word at 192");
 
+// The site offsets arrive by value and are written into the array's header
+// by the kernel itself, so a call issues no host-to-device copy.
 template <typename T>
-__global__ void __launch_bounds__(kOpThreads, 1) k_gate2_noalloc(ProgDesc P, DevOp op, char* scratch) {
+__global__ void __launch_bounds__(kOpThreads, 1)
+k_gate2_noalloc(ProgDesc P, DevOp op, char* scratch, int64_t* offs, int64_t hi_offset) {
   extern __shared__ __align__(16) char smem[];
   SmallSmem<T>* sm = reinterpret_cast<SmallSmem<T>*>(smem + Layout<T>::big);
   // the array keeps the previous call's contents: clear what must start at zero
   if (threadIdx.x < ST_COUNT) P.stats[threadIdx.x] = 0.0;
-  if (threadIdx.x == 0) *P.err = 0;
+  if (threadIdx.x == 0) {
+    *P.err = 0;
+    offs[0] = 0;
+    offs[1] = hi_offset;
+  }
   __syncthreads();
   op_gate2<T>(P, op, smem, sm, scratch);
 }
@@ -1383,6 +1428,14 @@ extern "C" int mps_gate2_apply_noalloc(int precision, int trunc_mode, int chi_ma
     return fail(MPS_ERR_UNSUPPORTED, "bond dimension above 64: the static scratch of the allocation-free "
                                      "entry point holds one 128 x 128 theta (512 KiB)");
   if (chi_max <= 0 || chi_max > kChiLimit) chi_max = kChiLimit;
+  {
+    // the hi site must start after the lo site, before and after the split
+    // (dl x 2 x dm in, dl x 2 x k out with k <= min(2 dl, 2 dr, chi_max))
+    const int kmax = std::min(std::min(2 * bonds[0], 2 * bonds[2]), chi_max);
+    const int64_t lo_in = 2LL * bonds[0] * bonds[1], lo_out = 2LL * bonds[0] * kmax;
+    if (hi_offset < std::max(lo_in, lo_out))
+      return fail(MPS_ERR_ARG, "hi_offset overlaps the lo site (it must be >= 2*dl*max(dm, k_max))");
+  }
   if (cutoff < 0.0) cutoff = trunc_mode == MPS_TRUNC_EXATN ? 2.2250738585072014e-308 : 1e-6;
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -1395,9 +1448,7 @@ extern "C" int mps_gate2_apply_noalloc(int precision, int trunc_mode, int chi_ma
   }
   cudaStream_t st = reinterpret_cast<cudaStream_t>(cuda_stream);
   // header: site offsets (2 x int64) at 0, stats (ST_COUNT doubles) at 64, error word at 192
-  const int64_t offs[2] = {0, hi_offset};
-  e = cudaMemcpyAsync(base, offs, sizeof(offs), cudaMemcpyHostToDevice, st);
-  if (e != cudaSuccess) return fail(MPS_ERR_CUDA, cudaGetErrorString(e));
+  int64_t* offs = reinterpret_cast<int64_t*>(base);
   ProgDesc P;
   std::memset(&P, 0, sizeof(P));
   P.sites = sites;
@@ -1420,9 +1471,9 @@ extern "C" int mps_gate2_apply_noalloc(int precision, int trunc_mode, int chi_ma
   for (int i = 0; i < 32; ++i) op.m[i] = gate[i];
   char* scratch = base + kNoAllocHeader;
   if (precision == MPS_PREC_FP64)
-    k_gate2_noalloc<double><<<1, kOpThreads, Layout<double>::smem, st>>>(P, op, scratch);
+    k_gate2_noalloc<double><<<1, kOpThreads, Layout<double>::smem, st>>>(P, op, scratch, offs, hi_offset);
   else
-    k_gate2_noalloc<float><<<1, kOpThreads, Layout<float>::smem, st>>>(P, op, scratch);
+    k_gate2_noalloc<float><<<1, kOpThreads, Layout<float>::smem, st>>>(P, op, scratch, offs, hi_offset);
   e = cudaGetLastError();
   if (e != cudaSuccess) return fail(MPS_ERR_CUDA, cudaGetErrorString(e));
   int herr = 0;

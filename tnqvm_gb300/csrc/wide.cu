@@ -34,7 +34,8 @@ struct G16 {
 };
 
 template <typename T>
-__global__ void k_theta_gate(const cx<T>* __restrict__ Tb, cx<T>* __restrict__ Th, int dl, int dr, G16 g) {
+__global__ void k_theta_gate(const cx<T>* __restrict__ Tb, cx<T>* __restrict__ Th, int dl, int dr, G16 g,
+                             int trim) {
   const int Cc = 2 * dr;
   for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < (int64_t)dl * dr;
        idx += (int64_t)gridDim.x * blockDim.x) {
@@ -48,6 +49,9 @@ __global__ void k_theta_gate(const cx<T>* __restrict__ Tb, cx<T>* __restrict__ T
 #pragma unroll
       for (int col = 0; col < 4; ++col)
         fma_c(acc, mk<T>(T(g.m[2 * (row * 4 + col)]), T(g.m[2 * (row * 4 + col) + 1])), t[col]);
+      // exatn semantics: moduli below 1e-100 become zero before the split
+      // (stabilizeTensorBody, ExaTnMpsVisitor.cpp:141-161); complex128 only
+      if (sizeof(T) == 8 && trim && (double)abs2(acc) < 1e-200) acc = mk<T>(T(0), T(0));
       Th[(int64_t)(2 * l + (row >> 1)) * Cc + (row & 1) * dr + r] = acc;
     }
   }
@@ -82,6 +86,43 @@ __global__ void k_split_scales(const double* lam, int k, int sqrt_mode, double r
       iso[j] = T(1);
       oth[j] = T(rn);
     }
+  }
+}
+
+// sqrt(S) on both sides (exatn semantics) from the unscaled other side O =
+// W_k^H X: sigma_j = |row j of O| (rows contiguous in a k x nn O, or column j
+// of an nn x k O^T), accurate to ~eps * sigma_max / sigma where sqrt of the
+// Gram eigenvalue is only accurate to ~eps * (sigma_max / sigma)^2 (ITensor
+// takes its singular values from the QR of M^H U, SVDRefImpl, tensor/
+// algs.cc:541-548).  A column whose eigenvalue counts as zero gets 0 on both
+// sides.  One block per kept column.
+template <typename T>
+__global__ void k_sqrt_scales(const cx<T>* O, int nn, int k, int transposed, const double* lam, double rn, T* iso,
+                              T* oth) {
+  __shared__ double red[32];
+  const int j = blockIdx.x;
+  double s2 = 0.0;
+  for (int c = threadIdx.x; c < nn; c += blockDim.x)
+    s2 += (double)abs2(transposed ? O[(int64_t)c * k + j] : O[(int64_t)j * nn + c]);
+  for (int o = 16; o > 0; o >>= 1) s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s2;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double tot = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += red[w];
+    const double h = lam[j] > 0.0 ? sqrt(sqrt(tot)) : 0.0;
+    iso[j] = T(h);
+    oth[j] = T(h > 0.0 ? rn / h : 0.0);
+  }
+}
+
+// Other side O scaled by oth per kept index (rows of k x nn, or columns of nn x k).
+template <typename T>
+__global__ void k_scale_other(cx<T>* O, int nn, int k, int transposed, const T* oth) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < (int64_t)k * nn;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int j = transposed ? (int)(t % k) : (int)(t / nn);
+    O[t] = scl(O[t], oth[j]);
   }
 }
 
@@ -477,7 +518,8 @@ static int wide_gate2(mps_prog* p, WideBufs& B, cudaStream_t st, const DevOp& op
             st));
   G16 g;
   std::memcpy(g.m, op.m, sizeof(g.m));
-  k_theta_gate<T><<<blocks_for((int64_t)dl * dr), 256, 0, st>>>(tb, theta, dl, dr, g);
+  k_theta_gate<T><<<blocks_for((int64_t)dl * dr), 256, 0, st>>>(tb, theta, dl, dr, g,
+                                                                 p->mode == TRUNC_EXATN ? 1 : 0);
   bool tr;
   if (op.orient == ORIENT_TO_HI)
     tr = false;
@@ -617,12 +659,24 @@ static int wide_gate2(mps_prog* p, WideBufs& B, cudaStream_t st, const DevOp& op
   const double rn = ((p->flags & MPS_FLAG_RENORM) && kept > 0.0) ? std::sqrt(total / kept) : 1.0;
   T* iso = reinterpret_cast<T*>(B.scal);
   T* oth = iso + B.m;
-  k_split_scales<T><<<(k + 255) / 256, 256, 0, st>>>(B.lam, k, op.orient == ORIENT_SQRT ? 1 : 0, rn, iso, oth);
   cx<T>* Wo = reinterpret_cast<cx<T>*>(Wf == reinterpret_cast<cx<T>*>(B.W2) ? B.W3 : B.W2);
-  if (!tr) {
+  if (op.orient == ORIENT_SQRT) {
+    // other side unscaled first, its row norms give the singular values
+    if (!tr)
+      WCK(cgemm(adj(cmat<T>(Wf, m, k, k, 1)), X, cout_<T>(Bs, k, Cc, Cc, 1), T(1), T(0), B.gemm, st));
+    else
+      WCK(cgemm(cmat<T>(theta, R, Cc, Cc, 1), cmat<T>(Wf, Cc, k, k, 1, 1), cout_<T>(A, R, k, k, 1), T(1), T(0),
+                B.gemm, st));
+    cx<T>* O = tr ? A : Bs;
+    k_sqrt_scales<T><<<k, 256, 0, st>>>(O, nn, k, tr ? 1 : 0, B.lam, rn, iso, oth);
+    k_scale_other<T><<<blocks_for((int64_t)k * nn), 256, 0, st>>>(O, nn, k, tr ? 1 : 0, oth);
+    k_write_iso<T><<<blocks_for((int64_t)m * k), 256, 0, st>>>(Wf, m, k, iso, oth, tr ? 1 : 0, tr ? Bs : A, Wo);
+  } else if (!tr) {
+    k_split_scales<T><<<(k + 255) / 256, 256, 0, st>>>(B.lam, k, 0, rn, iso, oth);
     k_write_iso<T><<<blocks_for((int64_t)m * k), 256, 0, st>>>(Wf, m, k, iso, oth, 0, A, Wo);
     WCK(cgemm(adj(cmat<T>(Wo, m, k, k, 1)), X, cout_<T>(Bs, k, Cc, Cc, 1), T(1), T(0), B.gemm, st));
   } else {
+    k_split_scales<T><<<(k + 255) / 256, 256, 0, st>>>(B.lam, k, 0, rn, iso, oth);
     k_write_iso<T><<<blocks_for((int64_t)m * k), 256, 0, st>>>(Wf, m, k, iso, oth, 1, Bs, Wo);
     WCK(cgemm(cmat<T>(theta, R, Cc, Cc, 1), cmat<T>(Wo, Cc, k, k, 1, 1), cout_<T>(A, R, k, k, 1), T(1), T(0),
               B.gemm, st));

@@ -209,21 +209,26 @@ class GpuMpsVisitor:
         """VQE mode: ``observed_circuit`` is the basis change plus Measure gates
         of one Pauli term (``TNQVM.cpp:82-89``).  The basis change is folded
         into a local Pauli on the resident MPS instead of re-simulating
-        (X basis: H, Y basis: Rx(pi/2), as XACC's observed composites emit)."""
+        (X basis: H, Y basis: Rx(pi/2), as XACC's observed composites emit).
+        Measuring Z after U measures U^H Z U, and Rx(t)^H Z Rx(t) = cos(t) Z +
+        sin(t) Y, so Rx(-pi/2) measures -Y."""
         n = self.buffer.size()
         letters = ["I"] * n
         pending = {}
+        sign = 1.0
         for name, qs, ps in observed_circuit:
             if name == "Measure":
                 q = qs[0]
-                letters[q] = pending.get(q, "Z")
+                letter, s = pending.get(q, ("Z", 1.0))
+                letters[q] = letter
+                sign *= s
             elif name == "H":
-                pending[qs[0]] = "X"
+                pending[qs[0]] = ("X", 1.0)
             elif name == "Rx" and abs(abs(ps[0]) - np.pi / 2) < 1e-12:
-                pending[qs[0]] = "Y"
+                pending[qs[0]] = ("Y", 1.0 if ps[0] > 0 else -1.0)
             else:
                 raise ValueError("unsupported basis-change gate %s" % name)
         if all(c == "I" for c in letters):
             return 0.0
         v = self.prog.expect_pauli(["".join(letters)])[0]
-        return float(v.real)
+        return sign * float(v.real)

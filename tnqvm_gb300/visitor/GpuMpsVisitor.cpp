@@ -183,11 +183,14 @@ void GpuMpsVisitor::finalize() {
 
 // VQE mode: the observed circuit is a basis change plus Measure on the
 // resident ansatz state (TNQVM.cpp:82-89); the basis change folds into a
-// local Pauli (H -> X, Rx(pi/2) -> Y) evaluated by the transfer-matrix sweep.
+// local Pauli evaluated by the transfer-matrix sweep.  Measuring Z after a
+// gate U measures U^H Z U: H -> X, and Rx(t)^H Z Rx(t) = cos(t) Z + sin(t) Y,
+// so Rx(pi/2) -> +Y and Rx(-pi/2) -> -Y.
 const double GpuMpsVisitor::getExpectationValueZ(std::shared_ptr<CompositeInstruction> function) {
   const int n = (int)buffer->size();
   std::string pauli(n, 'I');
-  std::map<int, char> basis;
+  std::map<int, std::pair<char, int>> basis;  // letter and sign per qubit
+  int sign = 1;
   bool any = false;
   xacc::InstructionIterator it(function);
   while (it.hasNext()) {
@@ -195,12 +198,14 @@ const double GpuMpsVisitor::getExpectationValueZ(std::shared_ptr<CompositeInstru
     if (!inst->isEnabled()) continue;
     const int q = (int)inst->bits()[0];
     if (inst->name() == "Measure") {
-      pauli[q] = basis.count(q) ? basis[q] : 'Z';
+      const auto b = basis.count(q) ? basis[q] : std::make_pair('Z', 1);
+      pauli[q] = b.first;
+      sign *= b.second;
       any = true;
     } else if (inst->name() == "H") {
-      basis[q] = 'X';
+      basis[q] = std::make_pair('X', 1);
     } else if (inst->name() == "Rx" && std::abs(std::abs(inst->getParameter(0)) - M_PI / 2) < 1e-12) {
-      basis[q] = 'Y';
+      basis[q] = std::make_pair('Y', inst->getParameter(0) > 0.0 ? 1 : -1);
     } else {
       throw std::runtime_error("gb300-mps: unsupported basis-change gate " + inst->name());
     }
@@ -208,7 +213,7 @@ const double GpuMpsVisitor::getExpectationValueZ(std::shared_ptr<CompositeInstru
   if (!any) return 0.0;
   double v[2];
   check(mps_expect_pauli(prog_, pauli.c_str(), 1, nullptr, v), "getExpectationValueZ");
-  return v[0];
+  return sign * v[0];
 }
 
 const std::vector<std::complex<double>> GpuMpsVisitor::getState() {

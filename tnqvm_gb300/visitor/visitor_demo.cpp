@@ -3,7 +3,10 @@
 // the AcceleratorBuffer contents as JSON.  Input on stdin, one gate per line:
 //   n_qubits shots
 //   <name> <nbits> <b0> [b1] <nparams> [p0 p1 p2]
-//   ... ; optional "opt <key> <value>" lines before the gates.
+//   ... ; optional "opt <key> <value>" lines before the gates, and
+//   "obs <name> <nbits> <b0> [b1] <nparams> [p...]" lines that form one
+//   observed circuit (basis change + Measure) whose VQE-mode value
+//   getExpectationValueZ returns (TNQVM.cpp:82-89) before finalize.
 #include <iostream>
 #include <sstream>
 
@@ -14,9 +17,15 @@ int main() {
   std::cin >> n >> shots;
   auto buffer = std::make_shared<xacc::AcceleratorBuffer>(n);
   auto program = std::make_shared<xacc::CompositeInstruction>("demo");
+  auto observed = std::make_shared<xacc::CompositeInstruction>("observed");
   xacc::HeterogeneousMap opts;
   std::string tok;
   while (std::cin >> tok) {
+    bool obs = false;
+    if (tok == "obs") {
+      obs = true;
+      std::cin >> tok;
+    }
     if (tok == "opt") {
       std::string key, val;
       std::cin >> key >> val;
@@ -32,7 +41,7 @@ int main() {
     std::cin >> np;
     std::vector<double> ps(np);
     for (auto& p : ps) std::cin >> p;
-    program->addInstruction(xacc::quantum::make_gate(tok, bits, ps));
+    (obs ? observed : program)->addInstruction(xacc::quantum::make_gate(tok, bits, ps));
   }
   auto visitor = std::make_shared<tnqvm::GpuMpsVisitor>();
   visitor->setOptions(opts);
@@ -42,9 +51,12 @@ int main() {
     auto inst = it.next();
     if (inst->isEnabled()) inst->accept(*visitor);
   }
+  const bool vqe = observed->nInstructions() > 0;
+  const double vqe_val = vqe ? visitor->getExpectationValueZ(observed) : 0.0;
   visitor->finalize();
   std::cout.precision(17);
   std::cout << "{\"name\": \"" << visitor->name() << "\"";
+  if (vqe) std::cout << ", \"vqe-exp-val\": " << vqe_val;
   for (auto& kv : buffer->getInformation()) {
     if (kv.second.type() == typeid(double))
       std::cout << ", \"" << kv.first << "\": " << std::any_cast<double>(kv.second);
