@@ -173,13 +173,14 @@ int mps_graph_timing(mps_graph* g, double out[6]);
  * truncation + split, out[4] centre moves. */
 int mps_graph_phase_cycles(mps_graph* g, double out[5]);
 /* Per-program statistics of the last replay summed over the graph's programs,
- * slots 0..n-1 (n <= 16): 0 sum log(1 - discarded fraction), 1 largest
+ * slots 0..n-1 (n <= 17): 0 sum log(1 - discarded fraction), 1 largest
  * discarded fraction (summed), 2 two-site splits, 3 ops, 4 GEMM-class flops,
  * 5 eigensolver flops, 6-10 the phase cycles of mps_graph_phase_cycles, 11
  * splits whose small-eigenvalue block was re-solved, 12-14 eigensolver cycles
  * in tridiagonalisation, bisection and eigenvector formation, 15 cycles of
- * orthonormalisation and the subspace step.  Diagnostics of this engine; no
- * counterpart in the reference. */
+ * orthonormalisation and the subspace step, 16 cycles of the attached
+ * observables (the Pauli sweeps after the gates).  Diagnostics of this
+ * engine; no counterpart in the reference. */
 int mps_graph_stat_sums(mps_graph* g, double* out, int n);
 int mps_graph_destroy(mps_graph* g);
 
@@ -282,6 +283,13 @@ int mps_autotune_tunings(mps_ctx* ctx, int* out);
  * chosen kernel; flags bit 0/1/2 store A/B/C column-major on the device. */
 int mps_diag_cgemm_kind(mps_ctx* ctx, int precision, int kernel, int flags, int M, int N, int K, const double* a,
                         const double* b, double* out);
+
+/* Diagnostic; no counterpart in the reference.  Peak fused multiply-add
+ * rate of the CUDA cores of `device` in one precision (MPS_PREC_FP32 or
+ * MPS_PREC_FP64), in flops/s (an FMA counts 2), from a probe kernel of
+ * independent FMA chains on every SM timed with CUDA events: the roofline
+ * denominator of the kernels that run on CUDA cores. */
+int mps_diag_fma_rate(int device, int precision, double* flops_per_s);
 
 /* Footprint used by admission: sum over sites of chi_l * 2 * chi_r * bytes. */
 size_t mps_footprint_bytes(int n_qubits, int chi_max, int precision);

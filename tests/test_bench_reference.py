@@ -1,6 +1,7 @@
 """bench.py's reference arm on CPU: ``--impl reference`` times the oracle
-port of the reference's MPS arithmetic on a bounded sample and prints one
-JSON line with the contract's keys (no GPU needed)."""
+port of the reference's MPS arithmetic on a fixed cost-stratified subset of
+the batch, one circuit per host core, and prints one JSON line with the
+contract's keys (no GPU needed)."""
 import json
 import os
 import subprocess
@@ -11,7 +12,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def test_reference_arm_prints_one_json_line():
     r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
-                        "--warmup", "0", "--ref-sample", "1"], capture_output=True, text=True, timeout=600,
+                        "--warmup", "0", "--ref-stride", "128"], capture_output=True, text=True, timeout=600,
                        cwd=ROOT)
     assert r.returncode == 0, r.stderr[-2000:]
     lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
@@ -19,5 +20,6 @@ def test_reference_arm_prints_one_json_line():
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["unit"] == "circuits/s" and d["value"] > 0
     assert d["higher_is_better"] is True and d["n_gpus"] == 1 and d["steps"] == 1
-    assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
+    assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] == (os.cpu_count() or 1)
+    assert d["config"]["instances_per_step"] == 8
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0

@@ -120,6 +120,41 @@ def test_hea_truncated_fp32_vs_fp64_oracle(ctx):
         assert abs(e - e_ref) < 1e-6
 
 
+def test_vqe_batch_accuracy_at_the_benchmark_config(ctx):
+    """The batched-VQE benchmark's own instances and settings (seed 2024, qubits
+    8..32, layers 4..12, bond cap 64, relative cutoff 1e-12, complex64, one
+    captured graph): the 16 costliest circuits of the 1024 plus 112 more
+    spread over the cost range, each |dE| <= 1e-6 against the complex128
+    itensor-mode oracle at the same cap and cutoff."""
+    from oracle.pool import OraclePool
+    insts = circuits.vqe_batch(1024, seed=2024)
+    order = np.argsort([it["n"] * it["layers"] for it in insts], kind="stable")
+    rest = order[:-16]
+    pick = sorted(set(int(i) for i in order[-16:]) |
+                  set(int(i) for i in rest[np.linspace(0, len(rest) - 1, 112).astype(int)]))
+    assert len(pick) == 128
+    sub = [insts[i] for i in pick]
+    progs = []
+    try:
+        for it in sub:
+            p = M.Program(ctx, it["n"], 64, 1e-12, M.TRUNC_ITENSOR, M.PREC_FP32)
+            p.record(M.encode_circuit(it["circuit"]))
+            p.set_observable(it["paulis"], it["coeffs"])
+            progs.append(p)
+        g = M.Graph(ctx, progs)
+        try:
+            got = g.launch()
+        finally:
+            g.close()
+    finally:
+        for p in progs:
+            p.close()
+    with OraclePool() as pool:
+        want, _, _ = pool.energies(sub, 64, 1e-12)
+    err = np.abs(np.asarray(got) - np.asarray(want))
+    assert err.max() <= 1e-6, (float(err.max()), pick[int(np.argmax(err))])
+
+
 # ------------------------------------------------- reference golden values
 def visitor_run(ctx, n, circ, shots=0, **opts):
     v = GpuMpsVisitor(ctx)

@@ -268,7 +268,7 @@ int mps_graph_phase_cycles(mps_graph* g, double out[5]) {
 
 int mps_graph_stat_sums(mps_graph* g, double* out, int n) {
   if (!g || !out) return fail(MPS_ERR_ARG, "NULL argument");
-  if (n < 1 || n > ST_COUNT) return fail(MPS_ERR_ARG, "n must be in 1..16");
+  if (n < 1 || n > ST_COUNT) return fail(MPS_ERR_ARG, "n must be in 1..17");
   GCK(cudaSetDevice(g->c->device));
   GCK(cudaStreamSynchronize(g->L.stream));
   for (int i = 0; i < n; ++i) out[i] = 0.0;

@@ -279,3 +279,77 @@ cudaError_t launch_reset(int prec, const ProgDesc* d_progs, int n_progs, cudaStr
   return cudaGetLastError();
 }
 }  // namespace gbmps
+
+// ------------------------------------------------ CUDA-core FMA rate probe
+// Peak fused multiply-add rate of the CUDA cores in one precision: every
+// thread runs eight independent chains a <- a * b + c (b slightly below 1,
+// so each chain settles at c / (1 - b) with no overflow), the grid fills
+// every SM eight CTAs deep.  The denominator of the roofline of kernels that
+// run on FP32/FP64 CUDA cores, measured on the GPU at hand.
+namespace gbmps {
+template <typename T>
+__global__ void __launch_bounds__(256) k_fma_rate(T* out, int iters, T b, T c) {
+  T a[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) a[i] = T(threadIdx.x + i);
+  for (int it = 0; it < iters; ++it) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) a[i] = fma(a[i], b, c);
+  }
+  T s = T(0);
+#pragma unroll
+  for (int i = 0; i < 8; ++i) s += a[i];
+  if (s == T(-1)) out[blockIdx.x] = s;  // never true; keeps the chains live
+}
+}  // namespace gbmps
+
+#include <string>
+
+#include "../../include/gb300mps.h"
+
+namespace gbmps {
+int fail(int code, const std::string& msg);
+}
+
+extern "C" int mps_diag_fma_rate(int device, int precision, double* flops_per_s) {
+  using namespace gbmps;
+  if (!flops_per_s) return fail(MPS_ERR_ARG, "NULL argument");
+  if (precision != MPS_PREC_FP64 && precision != MPS_PREC_FP32) return fail(MPS_ERR_ARG, "bad precision");
+  int prev = 0;
+  cudaError_t e = cudaGetDevice(&prev);
+  if (e == cudaSuccess) e = cudaSetDevice(device);
+  if (e != cudaSuccess) return fail(MPS_ERR_CUDA, cudaGetErrorString(e));
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  const int blocks = 8 * (sms > 0 ? sms : 1), threads = 256;
+  const int iters = precision == MPS_PREC_FP32 ? 1 << 16 : 1 << 11;
+  void* out = nullptr;
+  cudaStream_t st = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  float best = 0.0f;
+  e = cudaMalloc(&out, sizeof(double) * blocks);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  for (int rep = 0; rep < 4 && e == cudaSuccess; ++rep) {  // first launch is a warm-up
+    cudaEventRecord(e0, st);
+    if (precision == MPS_PREC_FP32)
+      k_fma_rate<float><<<blocks, threads, 0, st>>>(static_cast<float*>(out), iters, 0.999999f, 1e-6f);
+    else
+      k_fma_rate<double><<<blocks, threads, 0, st>>>(static_cast<double*>(out), iters, 0.999999, 1e-6);
+    cudaEventRecord(e1, st);
+    e = cudaEventSynchronize(e1);
+    float ms = 0.0f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    if (e == cudaSuccess && rep > 0 && (best == 0.0f || ms < best)) best = ms;
+  }
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e1) cudaEventDestroy(e1);
+  if (e0) cudaEventDestroy(e0);
+  if (st) cudaStreamDestroy(st);
+  if (out) cudaFree(out);
+  cudaSetDevice(prev);
+  if (e != cudaSuccess) return fail(MPS_ERR_CUDA, cudaGetErrorString(e));
+  *flops_per_s = 2.0 * 8.0 * iters * (double)blocks * threads / (best * 1e-3);
+  return MPS_OK;
+}

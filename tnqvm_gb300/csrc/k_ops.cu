@@ -1304,10 +1304,12 @@ k_run_ops(const ProgDesc* __restrict__ progs, int n_progs, int* queue, char* scr
       tk.bond = P.bond;
       tk.n = P.n;
       tk.pad = 0;
+      const long long c_obs = clock64();
       for (int t = 0; t < P.n_obs; ++t) {
         tk.codes = P.obs_codes + (size_t)t * P.n;
         expect_sweep<T>(tk, E, As, X, P.obs_out + 2 * t);
       }
+      if (threadIdx.x == 0) P.stats[ST_CYC_OBS] += (double)(clock64() - c_obs);
     }
     if (P.done != nullptr) {
       __syncthreads();
@@ -1360,7 +1362,7 @@ constexpr size_t kNoAllocHeader = 256;  // two site offsets, stats, error word
 constexpr size_t kNoAllocScratch = Layout<double>::scratch;  // largest per-CTA scratch (FP64)
 constexpr size_t kNoAllocBytes = kNoAllocHeader + kNoAllocScratch;  // 256 B + 512 KiB
 static __device__ __align__(256) char g_noalloc_scratch[kNoAllocBytes];
-static_assert(64 + sizeof(double) * ST_COUNT <= 192, "stats must end before the error word at 192");
+static_assert(64 + sizeof(double) * ST_COUNT <= 240, "stats must end before the error word at 240");
 
 // The site offsets arrive by value and are written into the array's header
 // by the kernel itself, so a call issues no host-to-device copy.
@@ -1447,7 +1449,7 @@ extern "C" int mps_gate2_apply_noalloc(int precision, int trunc_mode, int chi_ma
     return fail(MPS_ERR_CUDA, "cudaGetSymbolAddress / cudaFuncSetAttribute failed for the static scratch");
   }
   cudaStream_t st = reinterpret_cast<cudaStream_t>(cuda_stream);
-  // header: site offsets (2 x int64) at 0, stats (ST_COUNT doubles) at 64, error word at 192
+  // header: site offsets (2 x int64) at 0, stats (ST_COUNT doubles) at 64, error word at 240
   int64_t* offs = reinterpret_cast<int64_t*>(base);
   ProgDesc P;
   std::memset(&P, 0, sizeof(P));
@@ -1462,7 +1464,7 @@ extern "C" int mps_gate2_apply_noalloc(int precision, int trunc_mode, int chi_ma
   P.flags = 0;
   P.cutoff = cutoff;
   P.stats = reinterpret_cast<double*>(base + 64);
-  P.err = reinterpret_cast<int*>(base + 192);
+  P.err = reinterpret_cast<int*>(base + 240);
   DevOp op;
   std::memset(&op, 0, sizeof(op));
   op.kind = OP_GATE2;
@@ -1477,7 +1479,7 @@ extern "C" int mps_gate2_apply_noalloc(int precision, int trunc_mode, int chi_ma
   e = cudaGetLastError();
   if (e != cudaSuccess) return fail(MPS_ERR_CUDA, cudaGetErrorString(e));
   int herr = 0;
-  e = cudaMemcpyAsync(&herr, base + 192, sizeof(int), cudaMemcpyDeviceToHost, st);
+  e = cudaMemcpyAsync(&herr, base + 240, sizeof(int), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return fail(MPS_ERR_CUDA, cudaGetErrorString(e));
   if (herr & ERR_NAN) return fail(MPS_ERR_NUMERIC, "non-finite value in the two-site split");

@@ -98,7 +98,8 @@ enum StatSlot {
   ST_CYC_BISECT = 13, //   bisection and ranking of the eigenvalues
   ST_CYC_VEC = 14,    //   twisted-factorisation vectors and their back-transform
   ST_CYC_ORTH = 15,   // orthonormalisation and the subspace step (within the split phase)
-  ST_COUNT = 16,
+  ST_CYC_OBS = 16,    // attached observables evaluated by the program's CTA after its ops
+  ST_COUNT = 17,
 };
 
 // Error bits written by the kernels into ProgDesc::err.

@@ -80,6 +80,7 @@ SIGNATURES = [
                                             _P, _c.POINTER(_c.c_int), _DP, _P]),
     ("mps_diag_cgemm", _c.c_int, [_P, _c.c_int, _c.c_int, _c.c_int, _DP, _DP, _DP, _DP]),
     ("mps_diag_gemm_counts", _c.c_int, [_P, _c.POINTER(_c.c_int), _c.POINTER(_c.c_int)]),
+    ("mps_diag_fma_rate", _c.c_int, [_c.c_int, _c.c_int, _DP]),
     ("mps_diag_cgemm_kind", _c.c_int, [_P, _c.c_int, _c.c_int, _c.c_int, _c.c_int, _c.c_int, _c.c_int, _DP, _DP,
                                         _DP]),
     ("mps_autotune_set_mode", _c.c_int, [_c.c_int]),
@@ -256,6 +257,15 @@ class Context:
 
 
 # ---- GEMM autotuner of the wide path (process-wide table)
+def fma_rate(device=0, precision=PREC_FP32):
+    """Measured peak CUDA-core FMA rate (flops/s, an FMA counts 2) of one
+    precision on ``device``: the roofline denominator of CUDA-core kernels."""
+    load_library()
+    v = ctypes.c_double()
+    _check(_lib.mps_diag_fma_rate(device, precision, ctypes.byref(v)))
+    return v.value
+
+
 def autotune_set_mode(mode):
     """0 static rule, 1 tune new shape buckets, 2 tuned/loaded entries only."""
     load_library()
@@ -339,12 +349,13 @@ class Graph:
         return dict(zip(["theta", "gram", "eigensolver", "split", "moves"], out.tolist()))
 
     STAT_NAMES = ["log_fid", "max_disc", "gate2", "ops", "flops", "eig_flops", "cyc_theta", "cyc_gram",
-                  "cyc_eig", "cyc_split", "cyc_move", "refined", "cyc_trid", "cyc_bisect", "cyc_vec", "cyc_orth"]
+                  "cyc_eig", "cyc_split", "cyc_move", "refined", "cyc_trid", "cyc_bisect", "cyc_vec", "cyc_orth",
+                  "cyc_obs"]
 
     def stat_sums(self):
         """Per-program statistics of the last replay summed over the programs."""
-        out = np.zeros(16)
-        _check(_lib.mps_graph_stat_sums(self.h, _dptr(out), 16))
+        out = np.zeros(len(self.STAT_NAMES))
+        _check(_lib.mps_graph_stat_sums(self.h, _dptr(out), len(self.STAT_NAMES)))
         return dict(zip(self.STAT_NAMES, out.tolist()))
 
     @property
