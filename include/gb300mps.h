@@ -46,6 +46,15 @@ extern "C" {
 /* arithmetic */
 #define MPS_PREC_FP64 0 /* complex128 storage and arithmetic */
 #define MPS_PREC_FP32 1 /* complex64 storage and arithmetic, FP64 reductions */
+/* complex128 for a register of at most MPS_AUTO_FP64_QUBITS qubits whose bond
+ * cap is at least 2^floor(n/2) (the state is exact at that cap), complex64
+ * otherwise.  On small registers Pauli expectation values are O(1), and the
+ * rounding of complex64 arithmetic over a few hundred gates reaches ~1e-6 in
+ * a 50-term energy; those registers are also the cheapest to run in
+ * complex128.  A batch may mix the two (one persistent launch).  No
+ * counterpart in the reference (FP64 throughout). */
+#define MPS_PREC_AUTO 2
+#define MPS_AUTO_FP64_QUBITS 12
 
 /* program flags */
 #define MPS_FLAG_RENORM 1   /* rescale the kept part to the pre-truncation norm */
@@ -90,6 +99,8 @@ int mps_ctx_info(mps_ctx* ctx, int* num_sms, size_t* bytes_resident);
 int mps_program_begin(mps_ctx* ctx, int n_qubits, int chi_max, double cutoff,
                       int trunc_mode, int precision, int flags, mps_prog** out);
 int mps_program_reset(mps_prog* p); /* back to |0...0>, keeps the allocation */
+/* the precision the program runs in (MPS_PREC_AUTO resolved at begin) */
+int mps_program_precision(mps_prog* p, int* out);
 int mps_program_destroy(mps_prog* p);
 
 /* Gate recording.  Replaces the per-gate visit()/applyGate of

@@ -122,22 +122,24 @@ def test_hea_truncated_fp32_vs_fp64_oracle(ctx):
 
 def test_vqe_batch_accuracy_at_the_benchmark_config(ctx):
     """The batched-VQE benchmark's own instances and settings (seed 2024, qubits
-    8..32, layers 4..12, bond cap 64, relative cutoff 1e-12, complex64, one
-    captured graph): the 16 costliest circuits of the 1024 plus 112 more
-    spread over the cost range, each |dE| <= 1e-6 against the complex128
-    itensor-mode oracle at the same cap and cutoff."""
+    8..32, layers 4..12, bond cap 64, relative cutoff 1e-12, MPS_PREC_AUTO,
+    one captured graph): the 16 costliest circuits of the 1024, every circuit
+    of at most 13 qubits (the registers where complex64 rounding is largest)
+    and 112 more spread over the cost range, each |dE| <= 1e-6 against the
+    complex128 itensor-mode oracle at the same cap and cutoff."""
     from oracle.pool import OraclePool
     insts = circuits.vqe_batch(1024, seed=2024)
     order = np.argsort([it["n"] * it["layers"] for it in insts], kind="stable")
     rest = order[:-16]
-    pick = sorted(set(int(i) for i in order[-16:]) |
+    small = [i for i in range(len(insts)) if insts[i]["n"] <= 13]
+    pick = sorted(set(int(i) for i in order[-16:]) | set(small) |
                   set(int(i) for i in rest[np.linspace(0, len(rest) - 1, 112).astype(int)]))
-    assert len(pick) == 128
+    assert len(pick) >= 300
     sub = [insts[i] for i in pick]
     progs = []
     try:
         for it in sub:
-            p = M.Program(ctx, it["n"], 64, 1e-12, M.TRUNC_ITENSOR, M.PREC_FP32)
+            p = M.Program(ctx, it["n"], 64, 1e-12, M.TRUNC_ITENSOR, M.PREC_AUTO)
             p.record(M.encode_circuit(it["circuit"]))
             p.set_observable(it["paulis"], it["coeffs"])
             progs.append(p)
@@ -299,6 +301,44 @@ def test_batch_equals_individual(ctx):
         ref = omps.run(it["n"], it["circuit"], mode="itensor", chi_max=16, cutoff=0.0)
         er = sum(c * ref.expect_pauli(s).real for s, c in zip(it["paulis"], it["coeffs"])) / ref.norm2()
         assert abs(e - er) < 1e-5
+    for p in progs:
+        p.close()
+
+
+def test_mixed_precision_batch(ctx):
+    """MPS_PREC_AUTO: registers of at most 12 qubits whose cap keeps them exact
+    run in complex128, the others in complex64, in one persistent launch and
+    in one captured graph; every program gives what it gives alone in its
+    precision (1e-12) and matches the complex128 oracle (TOL64 for the
+    complex128 ones, TOL32 for the others)."""
+    insts = circuits.vqe_batch(instances=30, seed=12, qmin=6, qmax=18, lmin=2, lmax=6, terms=8)
+    progs = []
+    for it in insts:
+        p = M.Program(ctx, it["n"], 64, 1e-12, M.TRUNC_ITENSOR, M.PREC_AUTO)
+        p.record(M.encode_circuit(it["circuit"]))
+        p.set_observable(it["paulis"], it["coeffs"])
+        progs.append(p)
+    want_prec = [M.PREC_FP64 if it["n"] <= M.AUTO_FP64_QUBITS else M.PREC_FP32 for it in insts]
+    assert [p.precision for p in progs] == want_prec
+    assert len(set(want_prec)) == 2
+    g = M.Graph(ctx, progs)
+    try:
+        e_graph = np.array(g.launch())
+    finally:
+        g.close()
+    for p, it in zip(progs, insts):
+        p.record(M.encode_circuit(it["circuit"]))
+    ctx.batch_submit(progs)
+    e_batch = ctx.batch_expect(progs)
+    assert np.max(np.abs(e_batch - e_graph)) < 1e-12
+    for it, prec, e in zip(insts, want_prec, e_batch):
+        with M.Program(ctx, it["n"], 64, 1e-12, M.TRUNC_ITENSOR, prec) as p:
+            p.run(it["circuit"])
+            p.set_observable(it["paulis"], it["coeffs"])
+            assert abs(ctx.batch_expect([p])[0] - e) < 1e-12
+        ref = omps.run(it["n"], routing.route(it["circuit"]), mode="itensor", chi_max=64, cutoff=1e-12)
+        er = sum(c * ref.expect_pauli(s).real for s, c in zip(it["paulis"], it["coeffs"])) / ref.norm2()
+        assert abs(e - er) < (TOL64 if prec == M.PREC_FP64 else TOL32)
     for p in progs:
         p.close()
 

@@ -250,10 +250,9 @@ int lane_init(Lane& L) {
 void lane_free(Lane& L) {
   if (!L.stream) return;
   cudaStreamSynchronize(L.stream);
-  for (int p = 0; p < 2; ++p) {
-    if (L.op_scratch[p]) cudaFree(L.op_scratch[p]);
+  if (L.op_scratch) cudaFree(L.op_scratch);
+  for (int p = 0; p < 2; ++p)
     if (L.exp_scratch[p]) cudaFree(L.exp_scratch[p]);
-  }
   if (L.d_ops) cudaFree(L.d_ops);
   if (L.d_desc) cudaFree(L.d_desc);
   if (L.d_exp_tasks) cudaFree(L.d_exp_tasks);
@@ -297,11 +296,6 @@ int launch_programs(mps_ctx* c, Lane& L, mps_prog* const* progs_in, int n_in, bo
   if (n == 0) return MPS_OK;
   std::vector<std::vector<DevOp>> all(n);
   size_t total = 0;
-  int prec = -1;
-  for (int i = 0; i < n; ++i) {
-    if (prec < 0) prec = progs[i]->prec;
-    if (progs[i]->prec != prec) return fail(MPS_ERR_ARG, "batch mixes precisions");
-  }
   for (int i = 0; i < n; ++i) {
     compile_program(progs[i], all[i]);
     total += all[i].size();
@@ -336,6 +330,7 @@ int launch_programs(mps_ctx* c, Lane& L, mps_prog* const* progs_in, int n_in, bo
       d.chi_cap = p->chi_cap;
       d.mode = p->mode;
       d.flags = p->flags;
+      d.prec = p->prec;
       d.cutoff = p->cutoff;
       d.stats = p->d_stats;
       d.err = p->d_err;
@@ -375,19 +370,19 @@ int launch_programs(mps_ctx* c, Lane& L, mps_prog* const* progs_in, int n_in, bo
     if (e != cudaSuccess) return fail(MPS_ERR_CUDA, cudaGetErrorString(e));
     const int nd = (int)descs.size();
     if (per_gate) {
-      rc = ensure_bytes(&L.op_scratch[prec], &L.op_scratch_ctas[prec], 1, op_scratch_bytes(prec));
+      rc = ensure_bytes(&L.op_scratch, &L.op_scratch_ctas, 1, op_scratch_bytes());
       if (rc) return rc;
       for (int i = 0; i < nd; ++i) {
-        e = launch_ops(prec, L.d_desc + i, 1, 1, nullptr, L.op_scratch[prec], L.stream);
+        e = launch_ops(L.d_desc + i, 1, 1, nullptr, L.op_scratch, L.stream);
         if (e != cudaSuccess) return fail(MPS_ERR_CUDA, cudaGetErrorString(e));
       }
     } else {
       const int grid = std::min(nd, c->num_sms);
-      rc = ensure_bytes(&L.op_scratch[prec], &L.op_scratch_ctas[prec], c->num_sms, op_scratch_bytes(prec));
+      rc = ensure_bytes(&L.op_scratch, &L.op_scratch_ctas, c->num_sms, op_scratch_bytes());
       if (rc) return rc;
       e = cudaMemsetAsync(L.d_queue, 0, sizeof(int), L.stream);
       if (e != cudaSuccess) return fail(MPS_ERR_CUDA, cudaGetErrorString(e));
-      e = launch_ops(prec, L.d_desc, nd, grid, nd > 1 ? L.d_queue : nullptr, L.op_scratch[prec], L.stream);
+      e = launch_ops(L.d_desc, nd, grid, nd > 1 ? L.d_queue : nullptr, L.op_scratch, L.stream);
       if (e != cudaSuccess) return fail(MPS_ERR_CUDA, cudaGetErrorString(e));
     }
   }
@@ -640,13 +635,19 @@ int mps_program_begin(mps_ctx* c, int n, int chi_max, double cutoff, int trunc_m
   *out = nullptr;
   if (n < 1) return fail(MPS_ERR_ARG, "n_qubits must be >= 1");
   if (trunc_mode != MPS_TRUNC_EXATN && trunc_mode != MPS_TRUNC_ITENSOR) return fail(MPS_ERR_ARG, "bad trunc_mode");
-  if (precision != MPS_PREC_FP64 && precision != MPS_PREC_FP32) return fail(MPS_ERR_ARG, "bad precision");
+  if (precision != MPS_PREC_FP64 && precision != MPS_PREC_FP32 && precision != MPS_PREC_AUTO)
+    return fail(MPS_ERR_ARG, "bad precision");
   if (chi_max > MPS_WIDE_CHI_LIMIT)
     return fail(MPS_ERR_UNSUPPORTED, "max bond dimension above " + std::to_string(MPS_WIDE_CHI_LIMIT));
   if (chi_max > MPS_CHI_LIMIT && (flags & MPS_FLAG_PER_GATE))
     return fail(MPS_ERR_UNSUPPORTED, "the per-gate visitor path runs the single-CTA kernel (bond cap <= " +
                                          std::to_string(MPS_CHI_LIMIT) + ")");
   if (chi_max <= 0) chi_max = MPS_CHI_LIMIT;
+  if (precision == MPS_PREC_AUTO) {
+    // complex128 where the register is small and exact at its cap
+    const bool exact = n / 2 >= 30 || chi_max >= (1 << (n / 2));
+    precision = (n <= MPS_AUTO_FP64_QUBITS && exact) ? MPS_PREC_FP64 : MPS_PREC_FP32;
+  }
   std::lock_guard<std::mutex> lk(c->mu);
   CK(cudaSetDevice(c->device));
   mps_prog* p = new mps_prog();
@@ -692,6 +693,12 @@ int mps_program_begin(mps_ctx* c, int n, int chi_max, double cutoff, int trunc_m
   if (rc) return rc;
   c->resident += p->bytes;
   *out = p;
+  return MPS_OK;
+}
+
+int mps_program_precision(mps_prog* p, int* out) {
+  if (!p || !out) return fail(MPS_ERR_ARG, "NULL argument");
+  *out = p->prec;
   return MPS_OK;
 }
 

@@ -15,13 +15,13 @@
 namespace gbmps {
 
 // kernels (k_ops.cu, k_measure.cu)
-size_t op_scratch_bytes(int prec);
-size_t op_smem_bytes(int prec);
-cudaError_t launch_ops(int prec, const ProgDesc* d_progs, int n_progs, int grid, int* d_queue, char* scratch,
+size_t op_scratch_bytes();
+size_t op_smem_bytes();
+cudaError_t launch_ops(const ProgDesc* d_progs, int n_progs, int grid, int* d_queue, char* scratch,
                        cudaStream_t st);
 cudaError_t configure_ops();
 cudaError_t configure_expect();
-cudaError_t launch_reset(int prec, const ProgDesc* d_progs, int n_progs, cudaStream_t st);
+cudaError_t launch_reset(const ProgDesc* d_progs, int n_progs, cudaStream_t st);
 size_t expect_smem_bytes(int prec);
 size_t expect_scratch_bytes(int prec);
 cudaError_t launch_expect(int prec, const ExpTask* d_tasks, int n_tasks, char* scratch, double* d_out,
@@ -38,8 +38,8 @@ cudaError_t launch_amp_one(int prec, const void* sites, const int64_t* site_off,
 // different lanes can overlap on the device.
 struct Lane {
   cudaStream_t stream = nullptr;
-  char* op_scratch[2] = {nullptr, nullptr};
-  int op_scratch_ctas[2] = {0, 0};
+  char* op_scratch = nullptr;  // per-CTA scratch of the fused op kernel (either precision)
+  int op_scratch_ctas = 0;
   char* exp_scratch[2] = {nullptr, nullptr};
   int exp_scratch_ctas[2] = {0, 0};
   DevOp* d_ops = nullptr;

@@ -14,7 +14,6 @@ struct mps_graph {
   mps_ctx* c = nullptr;
   gbmps::Lane L;
   std::vector<mps_prog*> progs;
-  int prec = 0;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   std::vector<gbmps::DevOp> flat;
@@ -74,7 +73,6 @@ int mps_graph_create(mps_ctx* c, mps_prog* const* progs, int n, mps_graph** out)
   *out = nullptr;
   for (int i = 0; i < n; ++i) {
     if (!progs[i] || progs[i]->ctx != c) return fail(MPS_ERR_ARG, "program from another context");
-    if (progs[i]->prec != progs[0]->prec) return fail(MPS_ERR_ARG, "batch mixes precisions");
     if (prog_is_wide(progs[i]))
       return fail(MPS_ERR_UNSUPPORTED, "captured batches hold single-CTA programs (bond cap <= 64)");
   }
@@ -83,7 +81,6 @@ int mps_graph_create(mps_ctx* c, mps_prog* const* progs, int n, mps_graph** out)
   mps_graph* g = new mps_graph();
   g->c = c;
   g->progs.assign(progs, progs + n);
-  g->prec = progs[0]->prec;
   int rc = lane_init(g->L);
   if (rc) {
     delete g;
@@ -140,6 +137,7 @@ int mps_graph_create(mps_ctx* c, mps_prog* const* progs, int n, mps_graph** out)
     d.chi_cap = p->chi_cap;
     d.mode = p->mode;
     d.flags = p->flags;
+    d.prec = p->prec;
     d.cutoff = p->cutoff;
     d.stats = p->d_stats;
     d.err = p->d_err;
@@ -154,20 +152,19 @@ int mps_graph_create(mps_ctx* c, mps_prog* const* progs, int n, mps_graph** out)
     GCK(cudaMemcpy(L.d_ops, g->flat.data(), g->flat.size() * sizeof(DevOp), cudaMemcpyHostToDevice));
   GCK(cudaMemcpy(L.d_desc, descs.data(), descs.size() * sizeof(ProgDesc), cudaMemcpyHostToDevice));
   const int grid = std::min(n, c->num_sms);
-  const int prec = g->prec;
-  if (cudaMalloc(&L.op_scratch[prec], op_scratch_bytes(prec) * (size_t)grid) != cudaSuccess) {
+  if (cudaMalloc(&L.op_scratch, op_scratch_bytes() * (size_t)grid) != cudaSuccess) {
     cudaGetLastError();
     return bail(fail(MPS_ERR_OOM, "graph scratch allocation failed"));
   }
-  L.op_scratch_ctas[prec] = grid;
+  L.op_scratch_ctas = grid;
   cudaStream_t st = L.stream;
   for (int i = 0; i < 3; ++i)
     if (cudaEventCreate(&g->ev[i]) != cudaSuccess) return bail(fail(MPS_ERR_CUDA, "event creation failed"));
   GCK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
   cudaError_t e = cudaEventRecordWithFlags(g->ev[0], st, cudaEventRecordExternal);
-  if (e == cudaSuccess) e = launch_reset(prec, L.d_desc, n, st);
+  if (e == cudaSuccess) e = launch_reset(L.d_desc, n, st);
   if (e == cudaSuccess) e = cudaMemsetAsync(L.d_queue, 0, sizeof(int), st);
-  if (e == cudaSuccess) e = launch_ops(prec, L.d_desc, n, grid, n > 1 ? L.d_queue : nullptr, L.op_scratch[prec], st);
+  if (e == cudaSuccess) e = launch_ops(L.d_desc, n, grid, n > 1 ? L.d_queue : nullptr, L.op_scratch, st);
   if (e == cudaSuccess) e = cudaEventRecordWithFlags(g->ev[1], st, cudaEventRecordExternal);
   if (e == cudaSuccess && nt > 0)
     e = cudaMemcpyAsync(g->h_out, L.d_exp_out, 2 * (size_t)nt * sizeof(double), cudaMemcpyDeviceToHost, st);

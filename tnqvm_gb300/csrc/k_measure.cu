@@ -254,28 +254,33 @@ cudaError_t launch_amp_one(int prec, const void* sites, const int64_t* site_off,
 }  // namespace gbmps
 
 namespace gbmps {
-// Reset programs to |0...0> on the device: bonds 1, each site [1, 0], stats 0.
+// Reset programs to |0...0> on the device: bonds 1, each site [1, 0], stats
+// 0; each program in its own precision.
 template <typename T>
-__global__ void k_reset(const ProgDesc* __restrict__ progs, int n_progs) {
-  const int pi = blockIdx.x;
-  if (pi >= n_progs) return;
-  const ProgDesc P = progs[pi];
+__device__ void reset_sites(const ProgDesc& P) {
   cx<T>* sites = reinterpret_cast<cx<T>*>(P.sites);
   for (int i = threadIdx.x; i < P.n; i += blockDim.x) {
     sites[P.site_off[i]] = mk<T>(1, 0);
     sites[P.site_off[i] + 1] = mk<T>(0, 0);
   }
+}
+
+__global__ void k_reset(const ProgDesc* __restrict__ progs, int n_progs) {
+  const int pi = blockIdx.x;
+  if (pi >= n_progs) return;
+  const ProgDesc P = progs[pi];
+  if (P.prec == 0)
+    reset_sites<double>(P);
+  else
+    reset_sites<float>(P);
   for (int i = threadIdx.x; i <= P.n; i += blockDim.x) P.bond[i] = 1;
   if (threadIdx.x < ST_COUNT) P.stats[threadIdx.x] = 0.0;
   if (threadIdx.x == 0) *P.err = 0;
 }
 
-cudaError_t launch_reset(int prec, const ProgDesc* d_progs, int n_progs, cudaStream_t st) {
+cudaError_t launch_reset(const ProgDesc* d_progs, int n_progs, cudaStream_t st) {
   if (n_progs <= 0) return cudaSuccess;
-  if (prec == 0)
-    k_reset<double><<<n_progs, 64, 0, st>>>(d_progs, n_progs);
-  else
-    k_reset<float><<<n_progs, 64, 0, st>>>(d_progs, n_progs);
+  k_reset<<<n_progs, 64, 0, st>>>(d_progs, n_progs);
   return cudaGetLastError();
 }
 }  // namespace gbmps

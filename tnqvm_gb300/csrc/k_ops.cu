@@ -1251,102 +1251,116 @@ __device__ void op_move_l(const ProgDesc& P, const DevOp& op, char* big, SmallSm
   }
 }
 
+// One program on this CTA, in its own precision: its ops in order, then its
+// attached observables, then the completion flag of the serve loop.
 template <typename T>
+__device__ void run_program(const ProgDesc& P, char* smem, char* scratch) {
+  char* big = smem;
+  SmallSmem<T>* sm = reinterpret_cast<SmallSmem<T>*>(smem + Layout<T>::big);
+  for (int o = 0; o < P.n_ops; ++o) {
+    const DevOp& op = P.ops[o];
+    switch (op.kind) {
+      case OP_GATE1:
+        op_gate1<T>(P, op, sm);
+        break;
+      case OP_GATE2:
+        op_gate2<T>(P, op, big, sm, scratch);
+        break;
+      case OP_MOVE_R:
+        op_move_r<T>(P, op, big, sm, scratch);
+        break;
+      case OP_MOVE_L:
+        op_move_l<T>(P, op, big, sm, scratch);
+        break;
+      default:
+        break;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) P.stats[ST_N_OPS] += (double)P.n_ops;
+  if (P.n_obs > 0) {
+    // the program's observables on this CTA (the shared memory of the
+    // update is free now): per-request completion for the serve loop
+    using EL = ExpLayout<T>;
+    static_assert(EL::smem <= Layout<T>::big, "expectation work space must fit the update's shared memory");
+    static_assert(EL::scratch <= Layout<T>::scratch, "expectation scratch must fit the update's scratch");
+    cx<T>* E = reinterpret_cast<cx<T>*>(big);
+    cx<T>* As = E + EL::e_elems;
+    cx<T>* X = EL::staged ? As + EL::a_elems : reinterpret_cast<cx<T>*>(scratch);
+    ExpTask tk;
+    tk.sites = P.sites;
+    tk.site_off = P.site_off;
+    tk.bond = P.bond;
+    tk.n = P.n;
+    tk.pad = 0;
+    const long long c_obs = clock64();
+    for (int t = 0; t < P.n_obs; ++t) {
+      tk.codes = P.obs_codes + (size_t)t * P.n;
+      expect_sweep<T>(tk, E, As, X, P.obs_out + 2 * t);
+    }
+    if (threadIdx.x == 0) P.stats[ST_CYC_OBS] += (double)(clock64() - c_obs);
+  }
+  if (P.done != nullptr) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      P.done[1] = *(volatile int*)P.err;
+      __threadfence_system();
+      *(volatile int*)P.done = 1;
+    }
+  }
+}
+
+// The complex128 body is a separate call: its register allocation (which
+// spills) stays out of the complex64 body's.
+__device__ __noinline__ void run_program_f64(const ProgDesc& P, char* smem, char* scratch) {
+  run_program<double>(P, smem, scratch);
+}
+
+// Dynamic shared memory and global scratch per CTA of the persistent kernel:
+// enough for a program of either precision.
+constexpr size_t kOpsSmem = Layout<float>::smem > Layout<double>::smem ? Layout<float>::smem : Layout<double>::smem;
+constexpr size_t kOpsScratch =
+    Layout<float>::scratch > Layout<double>::scratch ? Layout<float>::scratch : Layout<double>::scratch;
+
+// Persistent: CTAs take programs from an atomic queue (longest first) until
+// it runs dry; each program runs in its own precision (ProgDesc::prec), so a
+// batch may mix complex64 and complex128 programs.
 __global__ void __launch_bounds__(kOpThreads, 1)
 k_run_ops(const ProgDesc* __restrict__ progs, int n_progs, int* queue, char* scratch_base, size_t scratch_stride) {
   extern __shared__ __align__(16) char smem[];
-  char* big = smem;
-  SmallSmem<T>* sm = reinterpret_cast<SmallSmem<T>*>(smem + Layout<T>::big);
+  __shared__ int next;
   char* scratch = scratch_base + scratch_stride * blockIdx.x;
   int pi = blockIdx.x;
   while (true) {
     if (queue != nullptr) {
-      if (threadIdx.x == 0) sm->ival[0] = atomicAdd(queue, 1);
+      if (threadIdx.x == 0) next = atomicAdd(queue, 1);
       __syncthreads();
-      pi = sm->ival[0];
+      pi = next;
       __syncthreads();
     }
     if (pi >= n_progs) break;
     const ProgDesc P = progs[pi];
-    for (int o = 0; o < P.n_ops; ++o) {
-      const DevOp& op = P.ops[o];
-      switch (op.kind) {
-        case OP_GATE1:
-          op_gate1<T>(P, op, sm);
-          break;
-        case OP_GATE2:
-          op_gate2<T>(P, op, big, sm, scratch);
-          break;
-        case OP_MOVE_R:
-          op_move_r<T>(P, op, big, sm, scratch);
-          break;
-        case OP_MOVE_L:
-          op_move_l<T>(P, op, big, sm, scratch);
-          break;
-        default:
-          break;
-      }
-      __syncthreads();
-    }
-    if (threadIdx.x == 0) P.stats[ST_N_OPS] += (double)P.n_ops;
-    if (P.n_obs > 0) {
-      // the program's observables on this CTA (the shared memory of the
-      // update is free now): per-request completion for the serve loop
-      using EL = ExpLayout<T>;
-      static_assert(EL::smem <= Layout<T>::big, "expectation work space must fit the update's shared memory");
-      static_assert(EL::scratch <= Layout<T>::scratch, "expectation scratch must fit the update's scratch");
-      cx<T>* E = reinterpret_cast<cx<T>*>(big);
-      cx<T>* As = E + EL::e_elems;
-      cx<T>* X = EL::staged ? As + EL::a_elems : reinterpret_cast<cx<T>*>(scratch);
-      ExpTask tk;
-      tk.sites = P.sites;
-      tk.site_off = P.site_off;
-      tk.bond = P.bond;
-      tk.n = P.n;
-      tk.pad = 0;
-      const long long c_obs = clock64();
-      for (int t = 0; t < P.n_obs; ++t) {
-        tk.codes = P.obs_codes + (size_t)t * P.n;
-        expect_sweep<T>(tk, E, As, X, P.obs_out + 2 * t);
-      }
-      if (threadIdx.x == 0) P.stats[ST_CYC_OBS] += (double)(clock64() - c_obs);
-    }
-    if (P.done != nullptr) {
-      __syncthreads();
-      if (threadIdx.x == 0) {
-        P.done[1] = *(volatile int*)P.err;
-        __threadfence_system();
-        *(volatile int*)P.done = 1;
-      }
-    }
+    if (P.prec == 0)
+      run_program_f64(P, smem, scratch);
+    else
+      run_program<float>(P, smem, scratch);
     if (queue == nullptr) break;
   }
 }
 
 // ------------------------------------------------------------- launchers
-template <typename T>
-static cudaError_t launch_ops_t(const ProgDesc* d_progs, int n_progs, int grid, int* d_queue, char* scratch,
-                                cudaStream_t st) {
-  k_run_ops<T><<<grid, kOpThreads, Layout<T>::smem, st>>>(d_progs, n_progs, d_queue, scratch, Layout<T>::scratch);
-  return cudaGetLastError();
-}
-
 // Opt in to the large dynamic shared memory once per device (outside any capture).
 cudaError_t configure_ops() {
-  cudaError_t e = cudaFuncSetAttribute(k_run_ops<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)Layout<float>::smem);
-  if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(k_run_ops<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)Layout<double>::smem);
+  return cudaFuncSetAttribute(k_run_ops, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kOpsSmem);
 }
 
-size_t op_scratch_bytes(int prec) { return prec == 0 ? Layout<double>::scratch : Layout<float>::scratch; }
-size_t op_smem_bytes(int prec) { return prec == 0 ? Layout<double>::smem : Layout<float>::smem; }
+size_t op_scratch_bytes() { return kOpsScratch; }
+size_t op_smem_bytes() { return kOpsSmem; }
 
-cudaError_t launch_ops(int prec, const ProgDesc* d_progs, int n_progs, int grid, int* d_queue, char* scratch,
+cudaError_t launch_ops(const ProgDesc* d_progs, int n_progs, int grid, int* d_queue, char* scratch,
                        cudaStream_t st) {
-  if (prec == 0) return launch_ops_t<double>(d_progs, n_progs, grid, d_queue, scratch, st);
-  return launch_ops_t<float>(d_progs, n_progs, grid, d_queue, scratch, st);
+  k_run_ops<<<grid, kOpThreads, kOpsSmem, st>>>(d_progs, n_progs, d_queue, scratch, kOpsScratch);
+  return cudaGetLastError();
 }
 
 // ------------------------------------------------- allocation-free variant

@@ -118,7 +118,7 @@ struct ProgDesc {
   int32_t chi_cap;
   int32_t mode;
   int32_t flags;
-  int32_t pad;
+  int32_t prec;             // 0 complex128, 1 complex64 (MPS_PREC_FP64 / MPS_PREC_FP32)
   double cutoff;
   double* stats;            // ST_COUNT doubles
   int* err;

@@ -15,7 +15,8 @@ LIB_PATH = os.path.join(_HERE, "_lib", "libgb300mps.so")
 
 OK, ERR_ARG, ERR_OOM, ERR_TIMEOUT, ERR_NUMERIC, ERR_CUDA, ERR_STATE, ERR_UNSUPPORTED = range(8)
 TRUNC_EXATN, TRUNC_ITENSOR = 0, 1
-PREC_FP64, PREC_FP32 = 0, 1
+PREC_FP64, PREC_FP32, PREC_AUTO = 0, 1, 2
+AUTO_FP64_QUBITS = 12
 FLAG_RENORM, FLAG_PER_GATE, FLAG_SWEEP = 1, 2, 4
 CHI_LIMIT = 64
 WIDE_CHI_LIMIT = 1024
@@ -41,6 +42,7 @@ SIGNATURES = [
     ("mps_program_begin", _c.c_int, [_P, _c.c_int, _c.c_int, _c.c_double, _c.c_int, _c.c_int, _c.c_int,
                                       _c.POINTER(_P)]),
     ("mps_program_reset", _c.c_int, [_P]),
+    ("mps_program_precision", _c.c_int, [_P, _c.POINTER(_c.c_int)]),
     ("mps_program_destroy", _c.c_int, [_P]),
     ("mps_gate1", _c.c_int, [_P, _c.c_int, _DP]),
     ("mps_gate2", _c.c_int, [_P, _c.c_int, _c.c_int, _DP]),
@@ -400,6 +402,13 @@ class Program:
 
     def reset(self):
         _check(_lib.mps_program_reset(self.h))
+
+    @property
+    def precision(self):
+        """The precision this program runs in (PREC_AUTO resolved)."""
+        v = ctypes.c_int()
+        _check(_lib.mps_program_precision(self.h, ctypes.byref(v)))
+        return v.value
 
     # ---- gates
     def gate(self, name, qubits, params=()):
