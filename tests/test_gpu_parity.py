@@ -327,6 +327,7 @@ def test_mixed_precision_batch(ctx):
     finally:
         g.close()
     for p, it in zip(progs, insts):
+        p.reset()  # the replay left the circuit's final state
         p.record(M.encode_circuit(it["circuit"]))
     ctx.batch_submit(progs)
     e_batch = ctx.batch_expect(progs)
