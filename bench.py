@@ -244,6 +244,9 @@ def run_ours(args):
     phase_share = {k: v / cyc_total for k, v in cycles.items()}
     phase_share["eigensolver_detail"] = {k: sums["cyc_" + k] / cyc_total for k in ("trid", "bisect", "vec")}
     phase_share["orthonormalise_in_split"] = sums["cyc_orth"] / cyc_total
+    # mean SM busy time (phase cycles summed over programs / SMs / clock)
+    # against the kernel's duration: the gap is the tail of the launch
+    busy_cycles = sum(cycles[k] for k in cycles)
     phase_share["refined_splits"] = int(sums["refined"])
     phase_share["splits"] = int(sums["gate2"])
     ms = max_over_ranks(ms, dist, "cuda")
@@ -313,6 +316,10 @@ def run_ours(args):
             "cuda_core_rates": rates,
             "phases_ms": {"reset_ops_and_observables": ops_ms, "copy_results": exp_ms},
             "fused_kernel_cycle_share": phase_share,
+            "load_balance": {"kernel_ms": ops_ms,
+                             "mean_sm_busy_ms": busy_cycles / ctx.num_sms / (1e3 * ((clocks or {}).get("sm_mhz")
+                                                                                   or 2070.0)),
+                             "complex128_programs": n_c128},
             "gpu_launches": 2 * args.steps,
             "clocks": clocks,
         }

@@ -276,6 +276,36 @@ static int ensure_bytes(char** ptr, int* have, int need, size_t per) {
   return MPS_OK;
 }
 
+// Estimated device time of a program on one CTA (arbitrary units) for the
+// longest-first order of the persistent launch: each two-site split ~ m^2 (m
+// + nn) at the sites' bond caps (Gram, tridiagonalisation, split; m the
+// smaller side), a centre move a fifth of that, the attached observables 2
+// chi_l chi_r (chi_l + chi_r) per site and term, and complex128 ~13x
+// complex64 (measured per program on GB300, FP64 at 1/63 of the FP32 rate).
+double program_cost(const mps_prog* p, const DevOp* ops, size_t n_ops, bool with_obs) {
+  const std::vector<int>& cap = p->cap_bond;
+  double c = 0.0;
+  for (size_t o = 0; o < n_ops; ++o) {
+    const int s = ops[o].site;
+    if (ops[o].kind == OP_GATE2 && s + 2 <= p->n) {
+      const double a = 2.0 * cap[s], b = 2.0 * cap[s + 2];
+      const double m = std::min(a, b), nn = std::max(a, b);
+      c += m * m * (m + nn);
+    } else if (ops[o].kind == OP_MOVE_R || ops[o].kind == OP_MOVE_L) {
+      const double d = (double)cap[s] * cap[s + 1];
+      c += 0.4 * d * std::max(cap[s], cap[s + 1]);
+    } else {
+      c += 8.0 * cap[s] * cap[s + 1];
+    }
+  }
+  if (with_obs) {
+    double sweep = 0.0;
+    for (int i = 0; i < p->n; ++i) sweep += 2.0 * cap[i] * cap[i + 1] * (double)(cap[i] + cap[i + 1]);
+    c += (p->n_terms + 1) * sweep;
+  }
+  return p->prec == MPS_PREC_FP64 ? 13.0 * c : c;
+}
+
 // Compile, upload and launch.  Non per-gate: one persistent launch whose CTAs
 // pull whole programs from an atomic queue (longest first).  Per-gate: one
 // single-CTA launch per op, the plain gate-by-gate visitor path.
@@ -351,10 +381,8 @@ int launch_programs(mps_ctx* c, Lane& L, mps_prog* const* progs_in, int n_in, bo
       std::vector<double> cost(n, 0.0);
       for (int i = 0; i < n; ++i) {
         order[i] = i;
-        const double cap = (double)progs[i]->chi_cap;
-        for (const DevOp& o : all[i]) cost[i] += (o.kind == OP_GATE2 ? 1.0 : 0.1) * cap * cap * cap;
-        if (progs[i]->serve_flag && progs[i]->d_obs)  // fused observables: ~a tenth of a split per site and term
-          cost[i] += 0.1 * (progs[i]->n_terms + 1) * progs[i]->n * cap * cap * cap;
+        cost[i] = program_cost(progs[i], all[i].data(), all[i].size(),
+                               progs[i]->serve_flag != nullptr && progs[i]->d_obs != nullptr);
       }
       std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[a] > cost[b]; });
       for (int i : order)

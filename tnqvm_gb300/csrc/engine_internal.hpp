@@ -173,6 +173,7 @@ void compile_program(::mps_prog* p, std::vector<DevOp>& ops);
 int lane_init(Lane& L);
 void lane_free(Lane& L);
 int launch_programs(mps_ctx* c, Lane& L, ::mps_prog* const* progs, int n, bool per_gate);
+double program_cost(const ::mps_prog* p, const DevOp* ops, size_t n_ops, bool with_obs);
 int enqueue_expect(Lane& L, const std::vector<ExpTask>& tasks, int prec, double* h_out);
 int enqueue_sample(Lane& L, ::mps_prog* p, int shots, uint64_t seed, uint8_t* h_all_bits);
 int prog_check_err(::mps_prog* p);

@@ -20,12 +20,13 @@ struct ExpLayout {
 // Transfer-matrix sweep of one Pauli string over one MPS (ITensor
 // compute_expectation_z, ITensorMPSVisitor.cpp:173-250, for any Pauli
 // letters): E <- sum_{l,s} A[l,s,:]^H (E P_s A)[l,s,:] site by site.  Step 1
-// forms Y = E A (dl x 2dr) in 4(l) x 4(r) x 2(s) register tiles (a tile's four
+// forms Y = E A (dl x 2dr) in 4(l) x 2(r) x 2(s) register tiles (a tile's two
 // columns are strided by the tile count, so a warp reads contiguous shared
-// memory without bank conflicts) and applies the
+// memory without bank conflicts; 512 tiles at bond 64, one per thread) and
+// applies the
 // site's Pauli as the 2x2 mix X[l,s,r] = sum_s' P[s,s'] Y[l,s',r] in
 // registers; step 2 forms E' = A_mat^H X (A_mat = A as a (2dl) x dr matrix) in
-// 4 x 4 tiles.  E (ld kChiLimit) and X are work space; As receives the
+// 4 x 2 tiles.  E (ld kChiLimit) and X are work space; As receives the
 // staged site when ExpLayout<T>::staged (else A is read from global memory).
 // Any block size; thread 0 writes <P> (re, im) to out2.  Called by every
 // thread of the block.
@@ -49,36 +50,38 @@ __device__ void expect_sweep(const ExpTask& tk, cx<T>* E, cx<T>* As, cx<T>* X, d
       A = Ag;
     }
     __syncthreads();
-    // step 1: X = P (E A), tiles of 4 rows l x 4 columns r x both s
+    // step 1: X = P (E A), tiles of 4 rows l x 2 columns r x both s (512
+    // tiles at bond 64: one per thread)
     {
-      const int nbl = (dl + 3) >> 2, nbr = (dr + 3) >> 2;
+      constexpr int TC = 2;
+      const int nbl = (dl + 3) >> 2, nbr = (dr + TC - 1) / TC;
       for (int tt = tid; tt < nbl * nbr; tt += nt) {
         const int bl = tt / nbr, br = tt - bl * nbr;
-        int el[4], ar[4];
+        int el[4], ar[TC];
 #pragma unroll
-        for (int a = 0; a < 4; ++a) {
-          el[a] = min(4 * bl + a, dl - 1) * LD;
-          ar[a] = min(br + a * nbr, dr - 1);  // columns strided by nbr: a warp's loads are contiguous
-        }
-        cx<T> y0[4][4], y1[4][4];
+        for (int a = 0; a < 4; ++a) el[a] = min(4 * bl + a, dl - 1) * LD;
+#pragma unroll
+        for (int b = 0; b < TC; ++b) ar[b] = min(br + b * nbr, dr - 1);  // columns strided by nbr: a warp's loads are contiguous
+        cx<T> y0[4][TC], y1[4][TC];
 #pragma unroll
         for (int a = 0; a < 4; ++a)
 #pragma unroll
-          for (int b = 0; b < 4; ++b) y0[a][b] = y1[a][b] = mk<T>(0, 0);
+          for (int b = 0; b < TC; ++b) y0[a][b] = y1[a][b] = mk<T>(0, 0);
         for (int lp = 0; lp < dl; ++lp) {
-          cx<T> e[4], a0[4], a1[4];
+          cx<T> e[4], a0[TC], a1[TC];
           const cx<T>* row0 = A + (lp * 2) * dr;
           const cx<T>* row1 = row0 + dr;
 #pragma unroll
-          for (int a = 0; a < 4; ++a) {
-            e[a] = E[el[a] + lp];
-            a0[a] = row0[ar[a]];
-            a1[a] = row1[ar[a]];
+          for (int a = 0; a < 4; ++a) e[a] = E[el[a] + lp];
+#pragma unroll
+          for (int b = 0; b < TC; ++b) {
+            a0[b] = row0[ar[b]];
+            a1[b] = row1[ar[b]];
           }
 #pragma unroll
           for (int a = 0; a < 4; ++a)
 #pragma unroll
-            for (int b = 0; b < 4; ++b) {
+            for (int b = 0; b < TC; ++b) {
               fma_c(y0[a][b], e[a], a0[b]);
               fma_c(y1[a][b], e[a], a1[b]);
             }
@@ -86,7 +89,7 @@ __device__ void expect_sweep(const ExpTask& tk, cx<T>* E, cx<T>* As, cx<T>* X, d
 #pragma unroll
         for (int a = 0; a < 4; ++a)
 #pragma unroll
-          for (int b = 0; b < 4; ++b) {
+          for (int b = 0; b < TC; ++b) {
             const int l = 4 * bl + a, r = br + b * nbr;
             if (l < dl && r < dr) {
               cx<T> x0 = y0[a][b], x1 = y1[a][b];
@@ -106,40 +109,40 @@ __device__ void expect_sweep(const ExpTask& tk, cx<T>* E, cx<T>* As, cx<T>* X, d
       }
     }
     __syncthreads();
-    // step 2: E'[r][r'] = sum_x conj(A[x][r]) X[x][r'], x = (l, s)
+    // step 2: E'[r][r'] = sum_x conj(A[x][r]) X[x][r'], x = (l, s), in 4 (r)
+    // x 2 (r') tiles (512 at bond 64)
     {
-      const int nb = (dr + 3) >> 2;
+      constexpr int TC = 2;
+      const int nbi = (dr + 3) >> 2, nbj = (dr + TC - 1) / TC;
       const int K = 2 * dl;
-      for (int tt = tid; tt < nb * nb; tt += nt) {
-        const int bi = tt / nb, bj = tt - bi * nb;
-        int ri[4], rj[4];
+      for (int tt = tid; tt < nbi * nbj; tt += nt) {
+        const int bi = tt / nbj, bj = tt - bi * nbj;
+        int ri[4], rj[TC];
 #pragma unroll
-        for (int a = 0; a < 4; ++a) {
-          ri[a] = min(4 * bi + a, dr - 1);
-          rj[a] = min(bj + a * nb, dr - 1);
-        }
-        cx<T> acc[4][4];
+        for (int a = 0; a < 4; ++a) ri[a] = min(4 * bi + a, dr - 1);
+#pragma unroll
+        for (int b = 0; b < TC; ++b) rj[b] = min(bj + b * nbj, dr - 1);
+        cx<T> acc[4][TC];
 #pragma unroll
         for (int a = 0; a < 4; ++a)
 #pragma unroll
-          for (int b = 0; b < 4; ++b) acc[a][b] = mk<T>(0, 0);
+          for (int b = 0; b < TC; ++b) acc[a][b] = mk<T>(0, 0);
         for (int x = 0; x < K; ++x) {
-          cx<T> av[4], xv[4];
+          cx<T> av[4], xv[TC];
 #pragma unroll
-          for (int a = 0; a < 4; ++a) {
-            av[a] = A[x * dr + ri[a]];
-            xv[a] = X[x * dr + rj[a]];
-          }
+          for (int a = 0; a < 4; ++a) av[a] = A[x * dr + ri[a]];
+#pragma unroll
+          for (int b = 0; b < TC; ++b) xv[b] = X[x * dr + rj[b]];
 #pragma unroll
           for (int a = 0; a < 4; ++a)
 #pragma unroll
-            for (int b = 0; b < 4; ++b) fma_cj(acc[a][b], av[a], xv[b]);
+            for (int b = 0; b < TC; ++b) fma_cj(acc[a][b], av[a], xv[b]);
         }
 #pragma unroll
         for (int a = 0; a < 4; ++a)
 #pragma unroll
-          for (int b = 0; b < 4; ++b) {
-            const int r = 4 * bi + a, rp = bj + b * nb;
+          for (int b = 0; b < TC; ++b) {
+            const int r = 4 * bi + a, rp = bj + b * nbj;
             if (r < dr && rp < dr) E[r * LD + rp] = acc[a][b];
           }
       }

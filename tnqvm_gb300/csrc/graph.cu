@@ -97,9 +97,7 @@ int mps_graph_create(mps_ctx* c, mps_prog* const* progs, int n, mps_graph** out)
   std::vector<double> cost(n, 0.0);
   for (int i = 0; i < n; ++i) {
     order[i] = i;
-    const double cap = (double)progs[i]->chi_cap;
-    for (size_t o = 0; o < g->count[i]; ++o)
-      cost[i] += (g->flat[g->first[i] + o].kind == OP_GATE2 ? 1.0 : 0.1) * cap * cap * cap;
+    cost[i] = program_cost(progs[i], g->flat.data() + g->first[i], g->count[i], progs[i]->d_obs != nullptr);
   }
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[a] > cost[b]; });
   Lane& L = g->L;

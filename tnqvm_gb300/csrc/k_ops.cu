@@ -35,13 +35,15 @@ struct Prec;
 // fits next to the packed Gram in shared memory (FP32), else it lives in the
 // CTA's global scratch (FP64, L2-resident).  refine: the FP32-only accuracy
 // steps of the split.  bisect_rounds: 5-section rounds, each shrinking the
-// bracket 5x, to reach ~eps of the spectrum's span.
+// bracket 5x, until it is below eps of the spectrum's span (5^-12 = 4e-9 <
+// 1.2e-7; 5^-24 = 1.7e-17 < 2.2e-16): Sturm counts cannot resolve an
+// eigenvalue more finely than that.
 template <>
 struct Prec<float> {
   static constexpr double eps = 1.1920929e-07;
   static constexpr bool u_in_smem = true;
   static constexpr bool refine = true;
-  static constexpr int bisect_rounds = 16;
+  static constexpr int bisect_rounds = 12;
   static constexpr double ns_stop = 1e-4;  // last Newton-Schulz step leaves ~1.5 ns_stop^2 < eps
   static constexpr double tri_flush = 1e-30;  // relative |column|^2 flushed in the tridiagonalisation
   static constexpr double tiny = 1e-36;       // absolute |column|^2 below which no reflector is formed
@@ -51,7 +53,7 @@ struct Prec<double> {
   static constexpr double eps = 2.220446049250313e-16;
   static constexpr bool u_in_smem = false;
   static constexpr bool refine = false;
-  static constexpr int bisect_rounds = 26;
+  static constexpr int bisect_rounds = 24;
   static constexpr double ns_stop = 1e-8;
   static constexpr double tri_flush = 1e-60;
   static constexpr double tiny = 1e-280;
@@ -353,6 +355,11 @@ __device__ void tridiagonalize(cx<T>* A, int m, double trace, SmallSmem<T>* sm) 
   __syncthreads();
 }
 
+// Quotient of the Sturm recurrence: only the signs of the pivots are used,
+// so FP32 takes the fast (2-ulp) division; |q| >= pivmin keeps it in range.
+__device__ __forceinline__ float sturm_div(float a, float b) { return __fdividef(a, b); }
+__device__ __forceinline__ double sturm_div(double a, double b) { return a / b; }
+
 // All eigenvalues of T (td, te): split into unreduced blocks, then each row j
 // finds the (j - block start)-th smallest eigenvalue of its block with four
 // lanes multisecting the interval (a fixed number of 5-section rounds).
@@ -410,7 +417,7 @@ __device__ void tri_bisect(int m, SmallSmem<T>* sm) {
     T qv = T(1);
     for (int i = s; i <= t; ++i) {
       const T e2 = i > s ? sm->te[i - 1] * sm->te[i - 1] : T(0);
-      qv = (sm->td[i] - x) - (i > s ? e2 / qv : T(0));
+      qv = (sm->td[i] - x) - (i > s ? sturm_div(e2, qv) : T(0));
       if (fabs(qv) < pivmin) qv = -pivmin;
       cnt += qv < T(0);
     }
