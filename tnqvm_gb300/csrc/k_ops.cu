@@ -35,15 +35,17 @@ struct Prec;
 // fits next to the packed Gram in shared memory (FP32), else it lives in the
 // CTA's global scratch (FP64, L2-resident).  refine: the FP32-only accuracy
 // steps of the split.  bisect_rounds: 5-section rounds, each shrinking the
-// bracket 5x, until it is below eps of the spectrum's span (5^-12 = 4e-9 <
-// 1.2e-7; 5^-24 = 1.7e-17 < 2.2e-16): Sturm counts cannot resolve an
-// eigenvalue more finely than that.
+// bracket 5x (5^-16 = 7e-12 of the span in FP32; 5^-24 = 1.7e-17 in FP64,
+// below eps: Sturm counts resolve an eigenvalue no more finely); with eight
+// lanes per eigenvalue (bisect_rounds9 9-section rounds) the bracket ends
+// at least as narrow.
 template <>
 struct Prec<float> {
   static constexpr double eps = 1.1920929e-07;
   static constexpr bool u_in_smem = true;
   static constexpr bool refine = true;
-  static constexpr int bisect_rounds = 12;
+  static constexpr int bisect_rounds = 16;
+  static constexpr int bisect_rounds9 = 12;  // 9^12 = 2.8e11 >= 5^16 = 1.5e11
   static constexpr double ns_stop = 1e-4;  // last Newton-Schulz step leaves ~1.5 ns_stop^2 < eps
   static constexpr double tri_flush = 1e-30;  // relative |column|^2 flushed in the tridiagonalisation
   static constexpr double tiny = 1e-36;       // absolute |column|^2 below which no reflector is formed
@@ -54,6 +56,7 @@ struct Prec<double> {
   static constexpr bool u_in_smem = false;
   static constexpr bool refine = false;
   static constexpr int bisect_rounds = 24;
+  static constexpr int bisect_rounds9 = 18;  // 9^18 = 1.5e17 >= 5^24 = 6.0e16
   static constexpr double ns_stop = 1e-8;
   static constexpr double tri_flush = 1e-60;
   static constexpr double tiny = 1e-280;
@@ -355,15 +358,62 @@ __device__ void tridiagonalize(cx<T>* A, int m, double trace, SmallSmem<T>* sm) 
   __syncthreads();
 }
 
-// Quotient of the Sturm recurrence: only the signs of the pivots are used,
-// so FP32 takes the fast (2-ulp) division; |q| >= pivmin keeps it in range.
-__device__ __forceinline__ float sturm_div(float a, float b) { return __fdividef(a, b); }
-__device__ __forceinline__ double sturm_div(double a, double b) { return a / b; }
-
 // All eigenvalues of T (td, te): split into unreduced blocks, then each row j
-// finds the (j - block start)-th smallest eigenvalue of its block with four
-// lanes multisecting the interval (a fixed number of 5-section rounds).
+// finds the (j - block start)-th smallest eigenvalue of its block with L
+// lanes multisecting the interval: L Sturm counts per round, the bracket
+// shrinks (L+1)-fold.  L = 4 (512 threads cover m = 128), or L = 8 when m <=
+// 64, where four lanes per eigenvalue would leave half the block idle.
 // Results: sm->lam[j] and the block bounds sm->bs[j], sm->bt[j].
+template <typename T, int L>
+__device__ void tri_multisect(int m, SmallSmem<T>* sm, int rounds) {
+  const int tid = threadIdx.x;
+  const T eps = T(Prec<T>::eps);
+  const int j = tid / L, q = tid % L;
+  const bool live = j < m;
+  const int s = live ? sm->bs[j] : 0, t = live ? sm->bt[j] : -1;
+  const int local = j - s;
+  T lo = T(0), hi = T(0), maxe2 = T(1);
+  for (int i = s; i <= t; ++i) {
+    const T el = i > s ? fabs(sm->te[i - 1]) : T(0), er = i < t ? fabs(sm->te[i]) : T(0);
+    const T d = sm->td[i];
+    if (i == s) {
+      lo = d - el - er;
+      hi = d + el + er;
+    } else {
+      lo = fmin(lo, d - el - er);
+      hi = fmax(hi, d + el + er);
+    }
+    maxe2 = fmax(maxe2, er * er);
+  }
+  const T pivmin = T(1.2e-38) * maxe2;
+  const T pad = T(4) * eps * fmax(fabs(lo), fabs(hi)) + pivmin;
+  T a = lo - pad, b = hi + pad;
+  const int base = threadIdx.x & 31 & ~(L - 1);
+  const unsigned gmask = ((1u << L) - 1u) << base;
+  for (int round = 0; round < rounds; ++round) {
+    const T w = (b - a) / T(L + 1);
+    const T x = a + w * T(q + 1);
+    int cnt = 0;
+    T qv = T(1);
+    for (int i = s; i <= t; ++i) {
+      const T e2 = i > s ? sm->te[i - 1] * sm->te[i - 1] : T(0);
+      qv = (sm->td[i] - x) - (i > s ? e2 / qv : T(0));
+      if (fabs(qv) < pivmin) qv = -pivmin;
+      cnt += qv < T(0);
+    }
+    // the new bracket ends at the first point whose count exceeds `local`
+    int first = L;
+#pragma unroll
+    for (int u = L - 1; u >= 0; --u)
+      if (__shfl_sync(gmask, cnt, base + u) > local) first = u;
+    const T na = first == 0 ? a : a + w * T(first);
+    const T nb = first == L ? b : a + w * T(first + 1);
+    a = na;
+    b = nb;
+  }
+  if (live && q == 0) sm->lam[j] = T(0.5) * (a + b);
+}
+
 template <typename T>
 __device__ void tri_bisect(int m, SmallSmem<T>* sm) {
   const int tid = threadIdx.x;
@@ -389,58 +439,10 @@ __device__ void tri_bisect(int m, SmallSmem<T>* sm) {
     }
   }
   __syncthreads();
-  const int j = tid >> 2, q = tid & 3;
-  const bool live = j < m;
-  const int s = live ? sm->bs[j] : 0, t = live ? sm->bt[j] : -1;
-  const int local = j - s;
-  T lo = T(0), hi = T(0), maxe2 = T(1);
-  for (int i = s; i <= t; ++i) {
-    const T el = i > s ? fabs(sm->te[i - 1]) : T(0), er = i < t ? fabs(sm->te[i]) : T(0);
-    const T d = sm->td[i];
-    if (i == s) {
-      lo = d - el - er;
-      hi = d + el + er;
-    } else {
-      lo = fmin(lo, d - el - er);
-      hi = fmax(hi, d + el + er);
-    }
-    maxe2 = fmax(maxe2, er * er);
-  }
-  const T pivmin = T(1.2e-38) * maxe2;
-  const T pad = T(4) * eps * fmax(fabs(lo), fabs(hi)) + pivmin;
-  T a = lo - pad, b = hi + pad;
-  const unsigned gmask = 0xFu << (threadIdx.x & 28);
-  for (int round = 0; round < Prec<T>::bisect_rounds; ++round) {
-    const T w = (b - a) / T(5);
-    const T x = a + w * T(q + 1);
-    int cnt = 0;
-    T qv = T(1);
-    for (int i = s; i <= t; ++i) {
-      const T e2 = i > s ? sm->te[i - 1] * sm->te[i - 1] : T(0);
-      qv = (sm->td[i] - x) - (i > s ? sturm_div(e2, qv) : T(0));
-      if (fabs(qv) < pivmin) qv = -pivmin;
-      cnt += qv < T(0);
-    }
-    const int base = threadIdx.x & 31 & ~3;
-    const int c0 = __shfl_sync(gmask, cnt, base + 0), c1 = __shfl_sync(gmask, cnt, base + 1);
-    const int c2 = __shfl_sync(gmask, cnt, base + 2), c3 = __shfl_sync(gmask, cnt, base + 3);
-    const T x0 = a + w * T(1), x1 = a + w * T(2), x2 = a + w * T(3), x3 = a + w * T(4);
-    if (c0 > local) {
-      b = x0;
-    } else if (c1 > local) {
-      a = x0;
-      b = x1;
-    } else if (c2 > local) {
-      a = x1;
-      b = x2;
-    } else if (c3 > local) {
-      a = x2;
-      b = x3;
-    } else {
-      a = x3;
-    }
-  }
-  if (live && q == 0) sm->lam[j] = T(0.5) * (a + b);
+  if (8 * m <= (int)blockDim.x)
+    tri_multisect<T, 8>(m, sm, Prec<T>::bisect_rounds9);
+  else
+    tri_multisect<T, 4>(m, sm, Prec<T>::bisect_rounds);
   __syncthreads();
 }
 
