@@ -360,6 +360,32 @@ def extra_measurements(args, ctx, insts, energies, value, world):
         "costliest_16_max_abs_dE": float(errs[order[-16:]].max()),
         "within_1e-6": int(np.sum(errs <= 1e-6)),
         "oracle": "complex128 itensor-mode MPS (LAPACK SVD), same cap and cutoff, every circuit of the batch"}
+    # the same batch with every register in complex128: the engine's mode for
+    # a bound on every circuit (complex64 misses 1e-6 where a truncation cuts
+    # through a nearly degenerate pair of singular values)
+    if args.fp64_batch:
+        progs = []
+        for it in insts:
+            p = M.Program(ctx, it["n"], CHI, CUTOFF, M.TRUNC_ITENSOR, M.PREC_FP64)
+            p.record(M.encode_circuit(it["circuit"]))
+            p.set_observable(it["paulis"], it["coeffs"])
+            progs.append(p)
+        g = M.Graph(ctx, progs)
+        try:
+            g.launch()
+            tms = []
+            for _ in range(2):
+                e64 = np.asarray(g.launch())
+                tms.append(g.timing()[0])
+        finally:
+            g.close()
+            for p in progs:
+                p.close()
+        err64 = np.abs(e64 - np.asarray(ref))
+        out["fp64_batch"] = {"value": len(insts) / (np.mean(tms) / 1e3), "unit": UNIT, "ms_per_step": float(np.mean(tms)),
+                             "max_abs_dE": float(err64.max()), "within_1e-6": int(np.sum(err64 <= 1e-6)),
+                             "what": "the same 1024 circuits, every register complex128, one captured replay, "
+                                     "device time"}
     out["cpu_baseline"] = {"value": len(insts) / wall, "unit": UNIT, "cores": cores, "kind": "port",
                            "sample": "the whole %d-circuit batch in %.1f s on %d worker processes (one circuit "
                                      "per process, single-threaded BLAS; %.1f core-seconds); numpy complex128 "
@@ -558,6 +584,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--instances", type=int, default=1024)
+    ap.add_argument("--fp64-batch", type=int, default=1, help="also time the batch all in complex128 (1/0)")
     ap.add_argument("--plain-sample", type=int, default=8)
     ap.add_argument("--plain-budget", type=float, default=60.0)
     ap.add_argument("--ref-stride", type=int, default=8,

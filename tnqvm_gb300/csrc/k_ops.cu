@@ -37,15 +37,14 @@ struct Prec;
 // steps of the split.  bisect_rounds: 5-section rounds, each shrinking the
 // bracket 5x (5^-16 = 7e-12 of the span in FP32; 5^-24 = 1.7e-17 in FP64,
 // below eps: Sturm counts resolve an eigenvalue no more finely); with eight
-// lanes per eigenvalue (bisect_rounds9 9-section rounds) the bracket ends
-// at least as narrow.
+// lanes per eigenvalue (bisect_rounds9 9-section rounds, FP64 with m <= 64)
+// the bracket ends at least as narrow.
 template <>
 struct Prec<float> {
   static constexpr double eps = 1.1920929e-07;
   static constexpr bool u_in_smem = true;
   static constexpr bool refine = true;
   static constexpr int bisect_rounds = 16;
-  static constexpr int bisect_rounds9 = 12;  // 9^12 = 2.8e11 >= 5^16 = 1.5e11
   static constexpr double ns_stop = 1e-4;  // last Newton-Schulz step leaves ~1.5 ns_stop^2 < eps
   static constexpr double tri_flush = 1e-30;  // relative |column|^2 flushed in the tridiagonalisation
   static constexpr double tiny = 1e-36;       // absolute |column|^2 below which no reflector is formed
@@ -439,10 +438,15 @@ __device__ void tri_bisect(int m, SmallSmem<T>* sm) {
     }
   }
   __syncthreads();
-  if (8 * m <= (int)blockDim.x)
-    tri_multisect<T, 8>(m, sm, Prec<T>::bisect_rounds9);
-  else
-    tri_multisect<T, 4>(m, sm, Prec<T>::bisect_rounds);
+  // eight lanes only in FP64, where each Sturm step's division is costly;
+  // FP32 keeps four lanes and its 5-section brackets (the complex64 results
+  // stay those the accuracy figures were measured with)
+  bool eight = false;
+  if constexpr (sizeof(T) == 8) {
+    eight = 8 * m <= (int)blockDim.x;
+    if (eight) tri_multisect<T, 8>(m, sm, Prec<T>::bisect_rounds9);
+  }
+  if (!eight) tri_multisect<T, 4>(m, sm, Prec<T>::bisect_rounds);
   __syncthreads();
 }
 
