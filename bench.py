@@ -196,7 +196,8 @@ def run_ours(args):
     rates = {"fp32_tflops": M.fma_rate(local, M.PREC_FP32) / 1e12,
              "fp64_tflops": M.fma_rate(local, M.PREC_FP64) / 1e12}
     rates["fp32_over_fp64"] = rates["fp32_tflops"] / rates["fp64_tflops"]
-    insts = circuits.vqe_batch(args.instances, seed=replica_seed(rank), qmax=args.qmax, lmax=args.lmax)
+    insts = circuits.vqe_batch(args.instances, seed=replica_seed(rank), qmin=args.qmin, qmax=args.qmax,
+                               lmax=args.lmax)
     t_enc = time.perf_counter()
     enc = [M.encode_circuit(it["circuit"]) for it in insts]
     encode_ms = 1e3 * (time.perf_counter() - t_enc)
@@ -419,8 +420,8 @@ def extra_measurements(args, ctx, insts, energies, value, world):
     # one large circuit on the wide path, and the mixed-cap serving stream
     if args.wide:
         out["wide_48q_chi512"] = wide_single(args, ctx)
-    if args.serve_mix > 0:
-        out["serve_mix"] = serve_mix(args, ctx)
+    if args.serve_stream > 0:
+        out["serve_stream"] = serve_stream(args, ctx)
     return out
 
 
@@ -494,49 +495,67 @@ def wide_single(args, ctx):
     return out
 
 
-def serve_mix(args, ctx):
-    """Poisson arrivals of random brick-wall circuits (qubits U{10..64},
-    depth U{10..40}, bond cap from {16, 64, 256, 512}), each returning 1024
-    shots and one Pauli expectation, through the continuous-batching loop
-    (caps above 64 on its wide lane)."""
+def serve_stream(args, ctx):
+    """The serving stream: Poisson arrivals at each offered rate of random
+    brick-wall circuits (qubits U{10..64}, depth U{10..40}, bond cap from
+    {16, 64, 256, 512}), each returning 1024 shots and one Pauli expectation,
+    through the continuous-batching loop (HBM admission under the 150 GB
+    budget; caps above 64 on its wide lane).  Every request with a cap <= 64
+    is followed by a parameter update: the same program, reset, re-recorded
+    with new angles and resubmitted, its MPS allocation reused."""
     from tnqvm_gb300 import circuits
     from tnqvm_gb300 import mps as M
-    rng = np.random.default_rng(44)
-    reqs = []
-    for i in range(args.serve_mix):
-        n = int(rng.integers(10, 65))
-        depth = int(rng.integers(10, 41))
-        chi = int(rng.choice([16, 64, 256, 512]))
-        p = M.Program(ctx, n, chi, 1e-10, M.TRUNC_ITENSOR, M.PREC_FP32)
-        p.run(circuits.brickwall(n, depth, seed=1000 + i))
-        s = "".join(rng.choice(list("IXYZ"), n))
-        p.set_observable([s], [1.0])
-        reqs.append((p, chi))
-    ctx.serve_start(256)
-    lats = {16: [], 64: [], 256: [], 512: []}
-    try:
-        gaps = rng.exponential(1.0 / args.serve_mix_rate, len(reqs))
-        tickets = []
-        t0 = time.perf_counter()
-        t_next = t0
-        for (p, chi), gap in zip(reqs, gaps):
-            t_next += gap
-            while time.perf_counter() < t_next:
-                pass
-            tickets.append(ctx.serve_submit(p, 1024, 7))
-        for (p, chi), t in zip(reqs, tickets):
-            _, _, lat = ctx.serve_poll(t, p, 1024)
-            lats[chi].append(lat)
-        wall = time.perf_counter() - t0
-    finally:
-        ctx.serve_stop()
-        for p, _ in reqs:
-            p.close()
-    allv = [x for v in lats.values() for x in v]
-    return {"requests": len(reqs), "offered_rate_per_s": args.serve_mix_rate, "circuits_per_s": len(reqs) / wall,
+    out = {"mode": "qubits U{10..64}, depth U{10..40}, cap {16,64,256,512}, 1024 shots + 1 Pauli term each; "
+                   "parameter updates on the resident programs of caps <= 64",
+           "requests_per_rate": args.serve_stream, "rates": []}
+    for ri, rate in enumerate(args.serve_rates):
+        rng = np.random.default_rng(44 + ri)
+        reqs = []
+        for i in range(args.serve_stream):
+            n = int(rng.integers(10, 65))
+            depth = int(rng.integers(10, 41))
+            chi = int(rng.choice([16, 64, 256, 512]))
+            p = M.Program(ctx, n, chi, 1e-10, M.TRUNC_ITENSOR, M.PREC_AUTO)
+            p.run(circuits.brickwall(n, depth, seed=1000 * ri + i))
+            p.set_observable(["".join(rng.choice(list("IXYZ"), n))], [1.0])
+            reqs.append((p, n, depth, chi))
+        ctx.serve_start(256)
+        lats = {16: [], 64: [], 256: [], 512: []}
+        upd = []
+        try:
+            gaps = rng.exponential(1.0 / rate, len(reqs))
+            tickets = []
+            t0 = time.perf_counter()
+            t_next = t0
+            for (p, n, depth, chi), gap in zip(reqs, gaps):
+                t_next += gap
+                while time.perf_counter() < t_next:
+                    pass
+                tickets.append(ctx.serve_submit(p, 1024, 7))
+            pending = []
+            for (p, n, depth, chi), t in zip(reqs, tickets):
+                _, _, lat = ctx.serve_poll(t, p, 1024)
+                lats[chi].append(lat)
+                if chi <= 64:  # parameter update on the resident program
+                    p.reset()
+                    p.run(circuits.brickwall(n, depth, seed=777 + len(pending)))
+                    pending.append((p, ctx.serve_submit(p, 1024, 8)))
+            for p, t in pending:
+                _, _, lat = ctx.serve_poll(t, p, 1024)
+                upd.append(lat)
+            wall = time.perf_counter() - t0
+        finally:
+            ctx.serve_stop()
+            for p, *_ in reqs:
+                p.close()
+        allv = [x for v in lats.values() for x in v] + upd
+        out["rates"].append({
+            "offered_rate_per_s": rate, "requests": len(allv), "wall_s": wall,
+            "achieved_per_s": len(allv) / wall,
             "p50_ms": float(np.percentile(allv, 50)), "p99_ms": float(np.percentile(allv, 99)),
             "p50_ms_by_cap": {str(k): float(np.percentile(v, 50)) for k, v in lats.items() if v},
-            "mode": "qubits U{10..64}, depth U{10..40}, cap {16,64,256,512}, 1024 shots + 1 Pauli term each"}
+            "parameter_updates": len(upd), "update_p50_ms": float(np.percentile(upd, 50)) if upd else None})
+    return out
 
 
 def serve_latency(args, ctx, insts, value):
@@ -598,8 +617,10 @@ def main():
                     help="layers of the 48-qubit circuit timed on the CPU oracle and on the GPU (0: off)")
     ap.add_argument("--wide-autotune", type=int, default=-1,
                     help="GEMM autotuner mode for the wide circuit (0 static, 1 tune, 2 table; -1 library default)")
-    ap.add_argument("--serve-mix", type=int, default=0, help="requests of the mixed-cap serving stream (0: off)")
-    ap.add_argument("--serve-mix-rate", type=float, default=100.0)
+    ap.add_argument("--serve-stream", type=int, default=12,
+                    help="requests per offered rate of the mixed-cap serving stream (0: off)")
+    ap.add_argument("--serve-rates", type=float, nargs="+", default=[1e2, 1e3, 1e4])
+    ap.add_argument("--qmin", type=int, default=8, help="smallest qubit count (small profiling cases)")
     ap.add_argument("--qmax", type=int, default=32, help="largest qubit count (small profiling cases)")
     ap.add_argument("--lmax", type=int, default=12, help="largest layer count (small profiling cases)")
     args = ap.parse_args()
