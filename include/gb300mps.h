@@ -55,6 +55,12 @@ extern "C" {
  * counterpart in the reference (FP64 throughout). */
 #define MPS_PREC_AUTO 2
 #define MPS_AUTO_FP64_QUBITS 12
+/* complex64 storage; the wide path's (bond caps above MPS_CHI_LIMIT)
+ * tensor-core products take bf16 operands split into head and remainder
+ * (three products, FP32 accumulation, ~1e-5 relative per product) at twice
+ * the TF32 rate; programs with caps <= MPS_CHI_LIMIT run as MPS_PREC_FP32.
+ * No counterpart in the reference. */
+#define MPS_PREC_SPLIT_BF16 3
 
 /* program flags */
 #define MPS_FLAG_RENORM 1   /* rescale the kept part to the pre-truncation norm */
@@ -62,6 +68,11 @@ extern "C" {
 #define MPS_FLAG_SWEEP 4    /* itensor semantics: reorder gates on disjoint qubits so the
                                orthogonality centre takes the shortest path (no reference
                                counterpart; truncations then happen in another order) */
+#define MPS_FLAG_FUSE 8     /* drop routed SWAP pairs that cancel (SWAP, 1-qubit gates on the
+                               pair, SWAP) and multiply consecutive 2-qubit gates on the same
+                               pair into one split (no reference counterpart: the reference
+                               splits after every routed SWAP; exact in exact arithmetic,
+                               fewer truncations otherwise) */
 
 /* largest bond dimension the single-CTA gate kernel handles */
 #define MPS_CHI_LIMIT 64
@@ -99,7 +110,8 @@ int mps_ctx_info(mps_ctx* ctx, int* num_sms, size_t* bytes_resident);
 int mps_program_begin(mps_ctx* ctx, int n_qubits, int chi_max, double cutoff,
                       int trunc_mode, int precision, int flags, mps_prog** out);
 int mps_program_reset(mps_prog* p); /* back to |0...0>, keeps the allocation */
-/* the precision the program runs in (MPS_PREC_AUTO resolved at begin) */
+/* the precision the program runs in (MPS_PREC_AUTO resolved at begin;
+ * MPS_PREC_SPLIT_BF16 reported as such) */
 int mps_program_precision(mps_prog* p, int* out);
 int mps_program_destroy(mps_prog* p);
 
@@ -291,7 +303,8 @@ int mps_autotune_clear(void);
 /* Buckets tuned by this context's wide workspaces so far. */
 int mps_autotune_tunings(mps_ctx* ctx, int* out);
 /* One product C = A B (host arrays of interleaved doubles, row-major) on a
- * chosen kernel; flags bit 0/1/2 store A/B/C column-major on the device. */
+ * chosen kernel; flags bit 0/1/2 store A/B/C column-major on the device, bit
+ * 3 runs the tensor-core kernel with split-BF16 operands. */
 int mps_diag_cgemm_kind(mps_ctx* ctx, int precision, int kernel, int flags, int M, int N, int K, const double* a,
                         const double* b, double* out);
 

@@ -108,6 +108,49 @@ def test_wide_exact_fp32(ctx, mode):
     assert t1 > t0  # the tensor-core kernel ran
 
 
+@pytest.mark.parametrize("layout", [0, 7])
+def test_split_bf16_gemm(ctx, layout):
+    """The tensor-core kernel with split-BF16 operands (kind::f16, bf16 head
+    and remainder, three products): within 6e-5 relative (Frobenius) of
+    numpy on a ragged product in row- and column-major storage, and not
+    equal to the 3xTF32 result (the other MMA kind ran)."""
+    rng = np.random.default_rng(17 + layout)
+    a = rng.standard_normal((257, 200)) + 1j * rng.standard_normal((257, 200))
+    b = rng.standard_normal((200, 131)) + 1j * rng.standard_normal((200, 131))
+    want = a @ b
+    got = ctx.diag_cgemm_kind(a, b, M.GEMM_TC, M.PREC_FP32, layout | 8)
+    tf32 = ctx.diag_cgemm_kind(a, b, M.GEMM_TC, M.PREC_FP32, layout)
+    rel = np.linalg.norm(got - want) / np.linalg.norm(want)
+    assert rel < 6e-5, rel
+    assert np.linalg.norm(tf32 - want) / np.linalg.norm(want) < 4e-6
+    assert np.max(np.abs(got - tf32)) > 0.0
+
+
+def test_split_bf16_program(ctx):
+    """MPS_PREC_SPLIT_BF16 on the exact 14-qubit circuit at cap 128 (wide
+    path, tensor-core products under the static rule): amplitudes within
+    2e-3 and <Z_q> within 1e-3 of the dense oracle; the program reports the
+    mode and the tensor-core kernel ran."""
+    n = 14
+    circ = circuits.brickwall(n, 14, seed=21)
+    psi = dense.run(n, circ)
+    old = M.autotune_mode()
+    M.autotune_set_mode(0)
+    try:
+        t0, _ = ctx.gemm_counts()
+        with run(ctx, n, circ, 128, 1e-14, M.TRUNC_ITENSOR, M.PREC_SPLIT_BF16) as p:
+            assert p.precision == M.PREC_SPLIT_BF16
+            amp = p.amplitudes()
+            assert np.max(np.abs(amp - psi)) < 2e-3
+            zs = p.expect_pauli(["I" * q + "Z" + "I" * (n - q - 1) for q in range(n)])
+            for q in range(n):
+                assert abs(zs[q].real - dense.expect_z_parity(psi, [q])) < 1e-3
+        t1, _ = ctx.gemm_counts()
+    finally:
+        M.autotune_set_mode(old)
+    assert t1 > t0
+
+
 def test_wide_routed_itensor_fp64(ctx):
     """Non-adjacent gates (SWAP routing) and centre moves in both directions:
     a 3-regular QAOA circuit on 14 qubits, cap 100, against the oracle."""

@@ -72,6 +72,7 @@ void compile_program(mps_prog* p, std::vector<DevOp>& ops) {
   routed.reserve(p->pending.size() * 2);
   for (const GateRec& g : p->pending) route_append(g, routed);
   p->pending.clear();
+  if (p->flags & MPS_FLAG_FUSE) cancel_swap_pairs(routed);
 
   struct Raw {
     int kind;
@@ -89,6 +90,11 @@ void compile_program(mps_prog* p, std::vector<DevOp>& ops) {
     m[3] = 1.0;
   };
   for (int q = 0; q < p->n; ++q) ident(&pend[4 * q]);
+  // MPS_FLAG_FUSE: the last raw op on each site, so that a 2-qubit gate on
+  // the pair its predecessor acted on (nothing else on either site in
+  // between) multiplies into that op instead of splitting again
+  const bool fuse = (p->flags & MPS_FLAG_FUSE) != 0;
+  std::vector<int> last(p->n, -1);
   for (const GateRec& g : routed) {
     if (g.nq == 1) {
       cd* P = &pend[4 * g.q0];
@@ -124,6 +130,19 @@ void compile_program(mps_prog* p, std::vector<DevOp>& ops) {
     ident(&pend[4 * lo]);
     ident(&pend[4 * (lo + 1)]);
     has[lo] = has[lo + 1] = 0;
+    const int k = last[lo];
+    if (fuse && k >= 0 && last[lo + 1] == k && raw[k].kind == OP_GATE2 && raw[k].site == lo) {
+      cd prod[16];
+      for (int row = 0; row < 4; ++row)
+        for (int col = 0; col < 4; ++col) {
+          cd acc = 0.0;
+          for (int q = 0; q < 4; ++q) acc += r.m[row * 4 + q] * raw[k].m[q * 4 + col];
+          prod[row * 4 + col] = acc;
+        }
+      for (int i = 0; i < 16; ++i) raw[k].m[i] = prod[i];
+      continue;
+    }
+    last[lo] = last[lo + 1] = (int)raw.size();
     raw.push_back(r);
   }
   for (int q = 0; q < p->n; ++q) {
@@ -663,14 +682,17 @@ int mps_program_begin(mps_ctx* c, int n, int chi_max, double cutoff, int trunc_m
   *out = nullptr;
   if (n < 1) return fail(MPS_ERR_ARG, "n_qubits must be >= 1");
   if (trunc_mode != MPS_TRUNC_EXATN && trunc_mode != MPS_TRUNC_ITENSOR) return fail(MPS_ERR_ARG, "bad trunc_mode");
-  if (precision != MPS_PREC_FP64 && precision != MPS_PREC_FP32 && precision != MPS_PREC_AUTO)
+  if (precision != MPS_PREC_FP64 && precision != MPS_PREC_FP32 && precision != MPS_PREC_AUTO &&
+      precision != MPS_PREC_SPLIT_BF16)
     return fail(MPS_ERR_ARG, "bad precision");
+  const int requested = precision;
   if (chi_max > MPS_WIDE_CHI_LIMIT)
     return fail(MPS_ERR_UNSUPPORTED, "max bond dimension above " + std::to_string(MPS_WIDE_CHI_LIMIT));
   if (chi_max > MPS_CHI_LIMIT && (flags & MPS_FLAG_PER_GATE))
     return fail(MPS_ERR_UNSUPPORTED, "the per-gate visitor path runs the single-CTA kernel (bond cap <= " +
                                          std::to_string(MPS_CHI_LIMIT) + ")");
   if (chi_max <= 0) chi_max = MPS_CHI_LIMIT;
+  if (precision == MPS_PREC_SPLIT_BF16) precision = MPS_PREC_FP32;  // complex64 storage
   if (precision == MPS_PREC_AUTO) {
     // complex128 where the register is small and exact at its cap
     const bool exact = n / 2 >= 30 || chi_max >= (1 << (n / 2));
@@ -684,6 +706,8 @@ int mps_program_begin(mps_ctx* c, int n, int chi_max, double cutoff, int trunc_m
   p->chi_cap = chi_max;
   p->mode = trunc_mode;
   p->prec = precision;
+  p->prec_mode = requested == MPS_PREC_AUTO ? precision : requested;
+  p->split_bf16 = requested == MPS_PREC_SPLIT_BF16;
   p->flags = flags;
   if (cutoff < 0.0) cutoff = trunc_mode == MPS_TRUNC_EXATN ? 2.2250738585072014e-308 : 1e-6;
   p->cutoff = cutoff;
@@ -726,7 +750,7 @@ int mps_program_begin(mps_ctx* c, int n, int chi_max, double cutoff, int trunc_m
 
 int mps_program_precision(mps_prog* p, int* out) {
   if (!p || !out) return fail(MPS_ERR_ARG, "NULL argument");
-  *out = p->prec;
+  *out = p->prec_mode;
   return MPS_OK;
 }
 
@@ -1128,10 +1152,11 @@ int mps_diag_cgemm_kind(mps_ctx* c, int precision, int kernel, int flags, int M,
                         const double* b, double* out) {
   if (!c || !a || !b || !out || M < 1 || N < 1 || K < 1 || M > 4096 || N > 4096 || K > 4096 || kernel < 0 ||
       kernel >= MPS_GEMM_KERNELS || (precision != MPS_PREC_FP64 && precision != MPS_PREC_FP32) || flags < 0 ||
-      flags > 7)
+      flags > 15)
     return fail(MPS_ERR_ARG, "bad argument");
   if (precision == MPS_PREC_FP64 && kernel == MPS_GEMM_TC)
     return fail(MPS_ERR_ARG, "the tensor-core GEMM takes complex64 only");
+  if ((flags & 8) && kernel != MPS_GEMM_TC) return fail(MPS_ERR_ARG, "split-BF16 applies to the tensor-core GEMM");
   std::lock_guard<std::mutex> lk(c->mu);
   CK(cudaSetDevice(c->device));
   return wide_diag_cgemm_kind(c, precision, kernel, flags, M, N, K, a, b, out);

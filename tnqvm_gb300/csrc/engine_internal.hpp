@@ -139,6 +139,8 @@ struct mps_ctx {
 struct mps_prog {
   mps_ctx* ctx = nullptr;
   int n = 0, chi_cap = 0, mode = 0, prec = 0, flags = 0;
+  int prec_mode = 0;        // the precision requested at begin (MPS_PREC_*), reported back
+  bool split_bf16 = false;  // wide-path tensor-core products with bf16 hi/lo operands
   double cutoff = 0.0;
   std::vector<gbmps::GateRec> pending;
   std::vector<int> measured;

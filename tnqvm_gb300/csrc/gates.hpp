@@ -5,6 +5,7 @@
 // index, Gates.hpp:238-246).  The router restates the meet-in-the-middle
 // strategy of tnqvm/visitors/exatn-mps/NearestNeighborTransform.hpp:43-135.
 #pragma once
+#include <algorithm>
 #include <cmath>
 #include <complex>
 #include <string>
@@ -150,6 +151,59 @@ inline void route_append(const GateRec& g, std::vector<GateRec>& out) {
   out.push_back(moved);
   for (int i = lo; i > lo0; --i) out.push_back(swap_rec(i, i - 1));
   for (int i = hi; i < hi0; ++i) out.push_back(swap_rec(i, i + 1));
+}
+
+// The exact SWAP of two neighbouring sites.
+inline bool is_adjacent_swap(const GateRec& g) {
+  if (g.nq != 2 || std::abs(g.q0 - g.q1) != 1) return false;
+  static const double S[16] = {1, 0, 0, 0, 0, 0, 1, 0, 0, 1, 0, 0, 0, 0, 0, 1};
+  for (int i = 0; i < 16; ++i)
+    if (g.m[i] != cd(S[i], 0.0)) return false;
+  return true;
+}
+
+// Peephole on a routed instruction stream (no reference counterpart; the
+// reference applies every SWAP of its meet-in-the-middle chains,
+// NearestNeighborTransform.hpp:83-121).  Two SWAPs on the same pair of
+// sites (a, a+1) with nothing in between that acts on a or a+1 except
+// 1-qubit gates are the identity: both are dropped and those 1-qubit gates
+// move to the other site of the pair (SWAP (A x B) SWAP = B x A).  Gates on
+// other sites commute with both SWAPs.  Scanning from the end removes nested
+// pairs (the return chain of one routed gate against the outgoing chain of
+// the next) innermost first.  Returns the number of SWAPs removed.
+inline size_t cancel_swap_pairs(std::vector<GateRec>& g) {
+  const size_t n = g.size();
+  std::vector<char> dead(n, 0);
+  std::vector<size_t> ones;
+  size_t removed = 0;
+  for (size_t i = n; i-- > 0;) {
+    if (dead[i] || !is_adjacent_swap(g[i])) continue;
+    const int a = std::min(g[i].q0, g[i].q1), b = a + 1;
+    ones.clear();
+    for (size_t j = i + 1; j < n; ++j) {
+      if (dead[j]) continue;
+      const GateRec& h = g[j];
+      const bool touch = h.q0 == a || h.q0 == b || (h.nq == 2 && (h.q1 == a || h.q1 == b));
+      if (!touch) continue;
+      if (h.nq == 1) {
+        ones.push_back(j);
+        continue;
+      }
+      if (is_adjacent_swap(h) && std::min(h.q0, h.q1) == a) {
+        dead[i] = dead[j] = 1;
+        removed += 2;
+        for (size_t k : ones) g[k].q0 = g[k].q0 == a ? b : a;
+      }
+      break;
+    }
+  }
+  if (removed) {
+    size_t w = 0;
+    for (size_t i = 0; i < n; ++i)
+      if (!dead[i]) g[w++] = g[i];
+    g.resize(w);
+  }
+  return removed;
 }
 
 // 4x4 re-expressed with its two qubits exchanged (row 2a+b -> 2b+a).

@@ -21,7 +21,16 @@
 // FP32 registers (4 x 128 columns = all 512 columns of tensor memory).
 // complex128 runs on a CUDA-core tiled kernel (FP64 has no fast tensor path
 // on this part).
+//
+// Split-BF16 (a program precision mode): the same pipeline on tcgen05
+// kind::f16 with bf16 operands, each split into a bf16 head and a bf16
+// remainder (~16 significant bits together) and the three products hi*hi +
+// hi*lo + lo*hi with FP32 accumulation: about twice the tensor rate of TF32
+// at ~1e-5 relative error per product instead of ~1e-6.  A 128-byte operand
+// row holds 32 fp32 or 64 bf16 values, so the tiles, swizzle and K steps (32
+// bytes, K = 8 tf32 or 16 bf16 per MMA) are the same in bytes.
 #include <cuda.h>
+#include <cuda_bf16.h>
 #include <cudaTypedefs.h>
 
 #include <cstdio>
@@ -158,6 +167,10 @@ constexpr int KP_ALIGN = 64;             // padded K (fp32) multiple of 64 (32 c
 // 7-9, 10-12 = 2), both K-major, N >> 3 at bit 17, M >> 4 at bit 24
 constexpr uint32_t IDESC = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(BN >> 3) << 17) |
                            ((uint32_t)(BM >> 4) << 24);
+// kind::f16 with bf16 A and B (bits 7-9, 10-12 = 1), D f32, both K-major
+constexpr uint32_t IDESC_BF16 = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
+                                ((uint32_t)(BM >> 4) << 24);
+constexpr int BK_BF16 = 64;              // bf16 K elements per stage (the same 128 B rows)
 constexpr long long kWaitNs = 2000000000LL;  // 2 s bound on every wait
 }  // namespace tc
 
@@ -214,6 +227,19 @@ __device__ __forceinline__ void umma_tf32(uint32_t tmem_d, uint64_t adesc, uint6
       " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
       "l"(adesc), "l"(bdesc), "r"(tc::IDESC), "r"(accum));
 }
+__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t accum) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(tc::IDESC_BF16), "r"(accum));
+}
+template <bool BF16>
+__device__ __forceinline__ void umma(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t accum) {
+  if (BF16)
+    umma_bf16(tmem_d, adesc, bdesc, accum);
+  else
+    umma_tf32(tmem_d, adesc, bdesc, accum);
+}
 __device__ __forceinline__ void umma_commit(uint64_t* bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
                : "memory");
@@ -230,7 +256,9 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
-// One 128 x 128 (real) output tile per CTA; 128 threads.
+// One 128 x 128 (real) output tile per CTA; 128 threads.  BF16: operands
+// are bf16 (64 per 128-byte row) and the MMAs kind::f16.
+template <bool BF16>
 __global__ void __launch_bounds__(128, 1)
     k_cgemm_tc(const __grid_constant__ CUtensorMap tm_ahi, const __grid_constant__ CUtensorMap tm_alo,
                const __grid_constant__ CUtensorMap tm_bhi, const __grid_constant__ CUtensorMap tm_blo, int k_tiles,
@@ -275,13 +303,16 @@ __global__ void __launch_bounds__(128, 1)
       if (*((volatile int*)flag)) break;
       uint8_t* st = smem + s * tc::STAGE;
       mbar_expect_tx(&full[s], tc::STAGE);
-      tma_load_2d(st + 0 * tc::TILE, &tm_ahi, kt * tc::BK, m0, &full[s]);
-      tma_load_2d(st + 1 * tc::TILE, &tm_alo, kt * tc::BK, m0, &full[s]);
-      tma_load_2d(st + 2 * tc::TILE, &tm_bhi, kt * tc::BK, n0, &full[s]);
-      tma_load_2d(st + 3 * tc::TILE, &tm_blo, kt * tc::BK, n0, &full[s]);
+      // x = the stage's first K element: 32 fp32 or 64 bf16 = 128 bytes per stage
+      const int kx = kt * (BF16 ? tc::BK_BF16 : tc::BK);
+      tma_load_2d(st + 0 * tc::TILE, &tm_ahi, kx, m0, &full[s]);
+      tma_load_2d(st + 1 * tc::TILE, &tm_alo, kx, m0, &full[s]);
+      tma_load_2d(st + 2 * tc::TILE, &tm_bhi, kx, n0, &full[s]);
+      tma_load_2d(st + 3 * tc::TILE, &tm_blo, kx, n0, &full[s]);
     }
   } else if (warp == 1 && lane == 0) {
-    // MMA issuer: 4 K-steps of 8 per stage, three products each
+    // MMA issuer: 4 K-steps of 32 bytes per stage (K = 8 tf32 or 16 bf16),
+    // three products each
     for (int kt = 0; kt < k_tiles; ++kt) {
       const int s = kt % tc::STAGES;
       const uint32_t ph = (uint32_t)(kt / tc::STAGES) & 1u;
@@ -298,9 +329,9 @@ __global__ void __launch_bounds__(128, 1)
         const uint32_t ko = (uint32_t)k * 32u;
         const uint64_t ahi = sw128_desc(base + 0 * tc::TILE + ko), alo = sw128_desc(base + 1 * tc::TILE + ko);
         const uint64_t bhi = sw128_desc(base + 2 * tc::TILE + ko), blo = sw128_desc(base + 3 * tc::TILE + ko);
-        umma_tf32(t_big, ahi, bhi, (kt >= tc::NBIG || k > 0) ? 1u : 0u);
-        umma_tf32(t_small, ahi, blo, (kt > 0 || k > 0) ? 1u : 0u);
-        umma_tf32(t_small, alo, bhi, 1u);
+        umma<BF16>(t_big, ahi, bhi, (kt >= tc::NBIG || k > 0) ? 1u : 0u);
+        umma<BF16>(t_small, ahi, blo, (kt > 0 || k > 0) ? 1u : 0u);
+        umma<BF16>(t_small, alo, bhi, 1u);
       }
       umma_commit(&empty[s]);
     }
@@ -394,6 +425,42 @@ __global__ void __launch_bounds__(256) k_pack(CMat<float> V, float* hi, float* l
   }
 }
 
+// The same packing into bf16 head and remainder: hi = bf16(x), lo =
+// bf16(x - hi), each rounded to nearest.
+template <bool BSIDE>
+__global__ void __launch_bounds__(256) k_pack_bf16(CMat<float> V, __nv_bfloat16* hi, __nv_bfloat16* lo, int kp) {
+  __shared__ cx<float> t[32][33];
+  const int r0 = blockIdx.y * 32, k0 = blockIdx.x * 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const bool lanes_r = BSIDE ? (V.cs == 1) : (V.rs == 1 && V.cs != 1);
+  for (int q = ty; q < 32; q += 8) {
+    const int rr = lanes_r ? tx : q, kk = lanes_r ? q : tx;
+    const int r = r0 + rr, k = k0 + kk;
+    t[rr][kk] = BSIDE ? vload(V, k, r) : vload(V, r, k);
+  }
+  __syncthreads();
+  for (int q = ty; q < 32; q += 8) {
+    const int r = r0 + q, k = k0 + tx;
+    const cx<float> z = t[q][tx];
+    const __nv_bfloat16 hr = __float2bfloat16_rn(z.re), hm = __float2bfloat16_rn(z.im);
+    const __nv_bfloat16 lr = __float2bfloat16_rn(z.re - __bfloat162float(hr));
+    const __nv_bfloat16 lm = __float2bfloat16_rn(z.im - __bfloat162float(hm));
+    const __nv_bfloat16 nhm = __float2bfloat16_rn(-__bfloat162float(hm));
+    const __nv_bfloat16 nlm = __float2bfloat16_rn(-__bfloat162float(lm));
+    if (!BSIDE) {
+      const int64_t o = (int64_t)r * kp + 2 * k;
+      *reinterpret_cast<__nv_bfloat162*>(hi + o) = __halves2bfloat162(hr, hm);
+      *reinterpret_cast<__nv_bfloat162*>(lo + o) = __halves2bfloat162(lr, lm);
+    } else {
+      const int64_t o0 = (int64_t)(2 * r) * kp + 2 * k, o1 = o0 + kp;
+      *reinterpret_cast<__nv_bfloat162*>(hi + o0) = __halves2bfloat162(hr, nhm);
+      *reinterpret_cast<__nv_bfloat162*>(lo + o0) = __halves2bfloat162(lr, nlm);
+      *reinterpret_cast<__nv_bfloat162*>(hi + o1) = __halves2bfloat162(hm, hr);
+      *reinterpret_cast<__nv_bfloat162*>(lo + o1) = __halves2bfloat162(lm, lr);
+    }
+  }
+}
+
 static PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
 static std::once_flag g_encode_once;
 static cudaError_t g_attr_err = cudaSuccess;
@@ -406,7 +473,9 @@ static bool get_encode() {
             cudaSuccess &&
         q == cudaDriverEntryPointSuccess)
       g_encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
-    g_attr_err = cudaFuncSetAttribute(k_cgemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM);
+    g_attr_err = cudaFuncSetAttribute(k_cgemm_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM);
+    if (g_attr_err == cudaSuccess)
+      g_attr_err = cudaFuncSetAttribute(k_cgemm_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM);
   });
   return g_encode != nullptr && g_attr_err == cudaSuccess;
 }
@@ -419,6 +488,17 @@ static bool make_map(CUtensorMap* m, float* base, int rows, int kp) {
   const cuuint32_t es[2] = {1, 1};
   return g_encode(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
                   CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// rows x kp bf16 row-major, box 64 (K) x 128 (rows): the same 128-byte rows
+static bool make_map_bf16(CUtensorMap* m, void* base, int rows, int kp) {
+  const cuuint64_t dims[2] = {(cuuint64_t)kp, (cuuint64_t)rows};
+  const cuuint64_t strides[1] = {(cuuint64_t)kp * 2};
+  const cuuint32_t box[2] = {(cuuint32_t)tc::BK_BF16, (cuuint32_t)tc::BM};
+  const cuuint32_t es[2] = {1, 1};
+  return g_encode(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides, box, es,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
@@ -466,14 +546,29 @@ static cudaError_t tc_launch(const CMat<float>& A, const CMat<float>& B, const C
   const int mp = (M + tc::BM - 1) / tc::BM * tc::BM;
   const int np = (2 * N + tc::BN - 1) / tc::BN * tc::BN;
   const int kp = (2 * K + tc::KP_ALIGN - 1) / tc::KP_ALIGN * tc::KP_ALIGN;
+  CUtensorMap ma, mal, mb, mbl;
+  if (ws.split_bf16) {
+    // bf16 operands in the same buffers (half the bytes)
+    auto* ahi = reinterpret_cast<__nv_bfloat16*>(ws.a_hi);
+    auto* alo = reinterpret_cast<__nv_bfloat16*>(ws.a_lo);
+    auto* bhi = reinterpret_cast<__nv_bfloat16*>(ws.b_hi);
+    auto* blo = reinterpret_cast<__nv_bfloat16*>(ws.b_lo);
+    k_pack_bf16<false><<<dim3(kp / 64, mp / 32), 256, 0, st>>>(A, ahi, alo, kp);
+    k_pack_bf16<true><<<dim3(kp / 64, np / 64), 256, 0, st>>>(B, bhi, blo, kp);
+    if (!make_map_bf16(&ma, ahi, mp, kp) || !make_map_bf16(&mal, alo, mp, kp) || !make_map_bf16(&mb, bhi, np, kp) ||
+        !make_map_bf16(&mbl, blo, np, kp))
+      return cudaErrorInvalidValue;
+    k_cgemm_tc<true><<<dim3(np / tc::BN, mp / tc::BM), 128, tc::SMEM, st>>>(ma, mal, mb, mbl, kp / tc::BK_BF16, C,
+                                                                           alpha, beta, ws.d_err);
+    return cudaGetLastError();
+  }
   k_pack<false><<<dim3(kp / 64, mp / 32), 256, 0, st>>>(A, ws.a_hi, ws.a_lo, kp);
   k_pack<true><<<dim3(kp / 64, np / 64), 256, 0, st>>>(B, ws.b_hi, ws.b_lo, kp);
-  CUtensorMap ma, mal, mb, mbl;
   if (!make_map(&ma, ws.a_hi, mp, kp) || !make_map(&mal, ws.a_lo, mp, kp) || !make_map(&mb, ws.b_hi, np, kp) ||
       !make_map(&mbl, ws.b_lo, np, kp))
     return cudaErrorInvalidValue;
-  k_cgemm_tc<<<dim3(np / tc::BN, mp / tc::BM), 128, tc::SMEM, st>>>(ma, mal, mb, mbl, kp / tc::BK, C, alpha, beta,
-                                                                    ws.d_err);
+  k_cgemm_tc<false><<<dim3(np / tc::BN, mp / tc::BM), 128, tc::SMEM, st>>>(ma, mal, mb, mbl, kp / tc::BK, C, alpha,
+                                                                           beta, ws.d_err);
   return cudaGetLastError();
 }
 
@@ -632,7 +727,8 @@ cudaError_t cgemm_tuned(const CMat<T>& A, const CMat<T>& B, const CMatOut<T>& C,
     int dev = 0;
     cudaGetDevice(&dev);
     // precision as in the C ABI: 0 complex128, 1 complex64
-    const uint32_t key = tune_key(dev, sizeof(T) == 8 ? 0 : 1, M, N, K, layout_bits(A, B, C));
+    const uint32_t key = tune_key(dev, sizeof(T) == 8 ? 0 : 1, M, N, K, layout_bits(A, B, C)) |
+                         (sizeof(T) == 4 && ws.split_bf16 ? (1u << 26) : 0u);
     bool found = false;
     {
       std::lock_guard<std::mutex> lk(g_tune_mu);
@@ -683,7 +779,7 @@ void gemm_tune_clear() {
 
 static void entry_row(uint32_t key, const TuneEntry& en, int* row) {
   row[0] = (int)((key >> 20) & 63);
-  row[1] = (int)((key >> 19) & 1);
+  row[1] = (key >> 26) & 1 ? 3 : (int)((key >> 19) & 1);  // 3: split-BF16 tensor-core products
   row[2] = (int)((key >> 15) & 15);
   row[3] = (int)((key >> 11) & 15);
   row[4] = (int)((key >> 7) & 15);
@@ -730,7 +826,7 @@ int gemm_tune_load(const char* path) {
     int n = sscanf(line, "%u %d %d %f %f %f %f %f", &key, &en.kind, &en.static_kind, &en.ns[0], &en.ns[1], &en.ns[2],
                    &en.ns[3], &en.ns[4]);
     if (n != 3 + GEMM_KINDS || en.kind < 0 || en.kind >= GEMM_KINDS || en.static_kind < 0 ||
-        en.static_kind >= GEMM_KINDS || (key >> 26) != 0) {
+        en.static_kind >= GEMM_KINDS || (key >> 27) != 0) {
       bad = true;
       break;
     }

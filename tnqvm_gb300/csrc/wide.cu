@@ -771,6 +771,7 @@ int wide_run(mps_ctx* c, Lane& L, mps_prog* p, void** ws) {
   WideBufs* B = nullptr;
   int rc = wide_bufs(ws ? ws : &c->wide, p->prec, p->chi_cap, &B);
   if (rc) return rc;
+  B->gemm.split_bf16 = p->split_bf16;  // tensor-core products of this program
   rc = p->prec == MPS_PREC_FP64 ? wide_run_t<double>(p, *B, L.stream, ops) : wide_run_t<float>(p, *B, L.stream, ops);
   if (rc) return rc;
   WCK(cudaEventRecord(p->ev, L.stream));
@@ -817,6 +818,7 @@ int wide_expect(mps_prog* p, const uint8_t* codes, int n_terms, double* out, Lan
   WideBufs* B = nullptr;
   int rc = wide_bufs(ws ? ws : &p->ctx->wide, p->prec, p->chi_cap, &B);
   if (rc) return rc;
+  B->gemm.split_bf16 = p->split_bf16;  // tensor-core products of this program
   cudaStream_t st = L ? L->stream : p->ctx->lane0.stream;
   return p->prec == MPS_PREC_FP64 ? wide_expect_t<double>(p, *B, st, codes, n_terms, out)
                                   : wide_expect_t<float>(p, *B, st, codes, n_terms, out);
@@ -887,6 +889,7 @@ int wide_sample(mps_prog* p, int shots, uint64_t seed, uint8_t* h_all_bits, Lane
   WideBufs* B = nullptr;
   int rc = wide_bufs(ws ? ws : &p->ctx->wide, p->prec, p->chi_cap, &B);
   if (rc) return rc;
+  B->gemm.split_bf16 = p->split_bf16;  // tensor-core products of this program
   cudaStream_t st = L ? L->stream : p->ctx->lane0.stream;
   return p->prec == MPS_PREC_FP64 ? wide_sample_t<double>(p, *B, st, shots, seed, h_all_bits)
                                   : wide_sample_t<float>(p, *B, st, shots, seed, h_all_bits);
@@ -917,6 +920,7 @@ int wide_amp_one(mps_prog* p, const int* bits, double* out) {
   WideBufs* B = nullptr;
   int rc = wide_bufs(&p->ctx->wide, p->prec, p->chi_cap, &B);
   if (rc) return rc;
+  B->gemm.split_bf16 = p->split_bf16;  // tensor-core products of this program
   cudaStream_t st = p->ctx->lane0.stream;
   return p->prec == MPS_PREC_FP64 ? wide_amp_one_t<double>(p, *B, st, bits, out)
                                   : wide_amp_one_t<float>(p, *B, st, bits, out);
@@ -991,6 +995,7 @@ static int wide_diag_cgemm_kind_t(mps_ctx* c, int kind, int flags, int M, int N,
   if (rc) return rc;
   cudaStream_t st = c->lane0.stream;
   const bool acm = flags & 1, bcm = flags & 2, ccm = flags & 4;
+  B->gemm.split_bf16 = sizeof(T) == 4 && (flags & 8);
   std::vector<cx<T>> ha((size_t)M * K), hb((size_t)K * N), hc((size_t)M * N);
   for (int i = 0; i < M; ++i)
     for (int k = 0; k < K; ++k) {

@@ -83,6 +83,7 @@ struct GemmWs {
   float* b_lo = nullptr;
   size_t a_elems = 0, b_elems = 0;
   int* d_err = nullptr;  // barrier/wait time-outs of the tensor-core kernel
+  bool split_bf16 = false;  // tensor-core products with bf16 hi/lo operands (MPS_PREC_SPLIT_BF16)
   int tc_launches = 0;   // tensor-core GEMM launches issued (diagnostics)
   int simt_launches = 0;
   // autotuner: output buffer of the trial launches and their timing events

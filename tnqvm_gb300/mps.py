@@ -15,9 +15,9 @@ LIB_PATH = os.path.join(_HERE, "_lib", "libgb300mps.so")
 
 OK, ERR_ARG, ERR_OOM, ERR_TIMEOUT, ERR_NUMERIC, ERR_CUDA, ERR_STATE, ERR_UNSUPPORTED = range(8)
 TRUNC_EXATN, TRUNC_ITENSOR = 0, 1
-PREC_FP64, PREC_FP32, PREC_AUTO = 0, 1, 2
+PREC_FP64, PREC_FP32, PREC_AUTO, PREC_SPLIT_BF16 = 0, 1, 2, 3
 AUTO_FP64_QUBITS = 12
-FLAG_RENORM, FLAG_PER_GATE, FLAG_SWEEP = 1, 2, 4
+FLAG_RENORM, FLAG_PER_GATE, FLAG_SWEEP, FLAG_FUSE = 1, 2, 4, 8
 CHI_LIMIT = 64
 WIDE_CHI_LIMIT = 1024
 # GEMM kernels of the wide path (MPS_GEMM_*) and the autotuner's row width
