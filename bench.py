@@ -495,6 +495,46 @@ def wide_single(args, ctx):
     return out
 
 
+def qaoa_precision(args):
+    """64-qubit QAOA MaxCut on a seeded random 3-regular graph (96 edges), p
+    rounds, gamma and beta uniform in [0, pi], RZZ as CNOT . Rz . CNOT, bond
+    cap 1024, cutoff 1e-12, itensor semantics with the routed SWAP pairs
+    cancelled and same-pair gates fused (MPS_FLAG_FUSE) and the gates swept
+    in centre order (MPS_FLAG_SWEEP): <H_cut> = sum over edges (1 - <Z_i
+    Z_j>)/2 in split-BF16, complex64 and complex128, each mode's error
+    against the complex128 run, seconds and truncation fidelity.  Off by
+    default (minutes per mode); ``--leg qaoa`` runs it alone."""
+    from tnqvm_gb300 import circuits
+    from tnqvm_gb300 import mps as M
+    n = 64
+    circ, edges = circuits.qaoa_maxcut(n=n, p=args.qaoa_p, seed=7)
+    terms = []
+    for a, b in edges:
+        s = ["I"] * n
+        s[a] = s[b] = "Z"
+        terms.append("".join(s))
+    with M.Context(env_int("LOCAL_RANK", 0)) as ctx:
+        out = {"workload": "64-qubit QAOA MaxCut, 3-regular graph (96 edges), p=%d, chi<=1024, cutoff 1e-12, "
+                           "itensor, fused routing + swept order" % args.qaoa_p}
+        vals = {}
+        for prec, key in ((M.PREC_FP64, "c128"), (M.PREC_FP32, "c64"), (M.PREC_SPLIT_BF16, "split_bf16")):
+            t0 = time.perf_counter()
+            p = M.Program(ctx, n, 1024, 1e-12, M.TRUNC_ITENSOR, prec, M.FLAG_FUSE | M.FLAG_SWEEP)
+            p.run(circ)
+            p.submit()
+            p.wait()
+            secs = time.perf_counter() - t0
+            zz = p.expect_pauli(terms).real / p.norm()
+            st = p.stats()
+            vals[key] = float(np.sum((1.0 - zz) / 2.0))
+            out[key] = {"seconds": secs, "H_cut": vals[key], "splits": st["gate2"], "max_bond": max(p.bond_dims()),
+                        "truncation_fidelity": float(st["fidelity"])}
+            p.close()
+        for key in ("c64", "split_bf16"):
+            out[key]["abs_err_H_cut_vs_c128"] = abs(vals[key] - vals["c128"])
+    return out
+
+
 def serve_stream(args, ctx):
     """The serving stream: Poisson arrivals at each offered rate of random
     brick-wall circuits (qubits U{10..64}, depth U{10..40}, bond cap from
@@ -623,9 +663,16 @@ def main():
     ap.add_argument("--qmin", type=int, default=8, help="smallest qubit count (small profiling cases)")
     ap.add_argument("--qmax", type=int, default=32, help="largest qubit count (small profiling cases)")
     ap.add_argument("--lmax", type=int, default=12, help="largest layer count (small profiling cases)")
+    ap.add_argument("--leg", default="", choices=["", "qaoa"],
+                    help="run one extra leg alone and print its JSON (qaoa: the 64-qubit precision comparison)")
+    ap.add_argument("--qaoa-p", type=int, default=3, help="QAOA rounds of the qaoa leg")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.leg == "qaoa":
+        build_locked()
+        print(json.dumps({"qaoa_precision": qaoa_precision(args)}))
+        return 0
     return run_ours(args)
 
 
