@@ -1268,6 +1268,7 @@ __device__ void op_move_l(const ProgDesc& P, const DevOp& op, char* big, SmallSm
 // attached observables, then the completion flag of the serve loop.
 template <typename T>
 __device__ void run_program(const ProgDesc& P, char* smem, char* scratch) {
+  const long long c_begin = clock64();
   char* big = smem;
   SmallSmem<T>* sm = reinterpret_cast<SmallSmem<T>*>(smem + Layout<T>::big);
   for (int o = 0; o < P.n_ops; ++o) {
@@ -1313,6 +1314,7 @@ __device__ void run_program(const ProgDesc& P, char* smem, char* scratch) {
     }
     if (threadIdx.x == 0) P.stats[ST_CYC_OBS] += (double)(clock64() - c_obs);
   }
+  if (P.cycles_out != nullptr && threadIdx.x == 0) *P.cycles_out = (double)(clock64() - c_begin);
   if (P.done != nullptr) {
     __syncthreads();
     if (threadIdx.x == 0) {

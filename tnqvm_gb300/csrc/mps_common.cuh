@@ -130,6 +130,9 @@ struct ProgDesc {
   int32_t pad2;
   double* obs_out;
   int* done;
+  // Optional: the program's SM clock cycles on its CTA (ops + observables),
+  // written when it finishes (captured batches order their next replay by it).
+  double* cycles_out;
 };
 
 // Measurement task descriptors (k_measure.cu).
