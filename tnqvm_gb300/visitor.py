@@ -117,7 +117,8 @@ class GpuMpsVisitor:
             self.ctx = default_context()
         o = self.options
         mode = {"exatn": M.TRUNC_EXATN, "itensor": M.TRUNC_ITENSOR}[o.get("truncation-mode", "exatn")]
-        prec = {"fp64": M.PREC_FP64, "fp32": M.PREC_FP32}[o.get("precision", "fp64")]
+        prec = {"fp64": M.PREC_FP64, "fp32": M.PREC_FP32, "auto": M.PREC_AUTO,
+                "split-bf16": M.PREC_SPLIT_BF16}[o.get("precision", "fp64")]
         flags = (M.FLAG_RENORM if o.get("renormalize", False) else 0) | \
                 (M.FLAG_PER_GATE if o.get("per-gate", False) else 0)
         cutoff = float(o["svd-cutoff"]) if "svd-cutoff" in o else -1.0

@@ -60,8 +60,15 @@ void GpuMpsVisitor::initialize(std::shared_ptr<AcceleratorBuffer> in_buffer, int
       options.get<std::string>("truncation-mode") == "itensor")
     mode = MPS_TRUNC_ITENSOR;
   int prec = MPS_PREC_FP64;
-  if (options.keyExists<std::string>("precision") && options.get<std::string>("precision") == "fp32")
-    prec = MPS_PREC_FP32;
+  if (options.keyExists<std::string>("precision")) {
+    const std::string v = options.get<std::string>("precision");
+    if (v == "fp32")
+      prec = MPS_PREC_FP32;
+    else if (v == "auto")
+      prec = MPS_PREC_AUTO;
+    else if (v == "split-bf16")
+      prec = MPS_PREC_SPLIT_BF16;
+  }
   int flags = 0;
   if (options.keyExists<bool>("renormalize") && options.get<bool>("renormalize")) flags |= MPS_FLAG_RENORM;
   if (options.keyExists<bool>("per-gate") && options.get<bool>("per-gate")) flags |= MPS_FLAG_PER_GATE;
