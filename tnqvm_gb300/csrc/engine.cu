@@ -257,9 +257,16 @@ void compile_program(mps_prog* p, std::vector<DevOp>& ops) {
   p->center = center;
 }
 
-int lane_init(Lane& L) {
+int lane_init(Lane& L, int priority) {
   if (L.stream) return MPS_OK;
-  cudaError_t e = cudaStreamCreateWithFlags(&L.stream, cudaStreamNonBlocking);
+  // priority > 0: the device's highest stream priority, < 0: its lowest, 0: default
+  int least = 0, greatest = 0;
+  if (priority != 0 && cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess) {
+    cudaGetLastError();
+    least = greatest = 0;
+  }
+  const int prio = priority > 0 ? greatest : priority < 0 ? least : 0;
+  cudaError_t e = cudaStreamCreateWithPriority(&L.stream, cudaStreamNonBlocking, prio);
   if (e != cudaSuccess) return fail(MPS_ERR_CUDA, cudaGetErrorString(e));
   e = cudaMalloc(&L.d_queue, 64 * sizeof(int));
   if (e != cudaSuccess) return fail(MPS_ERR_OOM, cudaGetErrorString(e));

@@ -101,13 +101,14 @@ struct ServeBatch {
 
 struct ServeState {
   std::thread worker;
-  // wide requests (bond cap above the single-CTA limit) run one at a time on
-  // their own worker, lane and workspace, overlapping the batched lanes
-  std::thread wide_worker;
+  // wide requests (bond cap above the single-CTA limit) run on their own
+  // workers, each with its lane and workspace, overlapping the batched lanes
+  // and one another
+  std::vector<std::thread> wide_workers;
   std::deque<ServeReq*> wide_queue;
   std::condition_variable cv_wide;
-  Lane wide_lane;
-  void* wide_ws = nullptr;
+  std::vector<Lane> wide_lanes;
+  std::vector<void*> wide_ws;
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
   std::deque<ServeReq*> queue;
@@ -172,7 +173,7 @@ extern thread_local std::string g_err;
 int fail(int code, const std::string& msg);
 size_t footprint(int n, int chi, int prec);
 void compile_program(::mps_prog* p, std::vector<DevOp>& ops);
-int lane_init(Lane& L);
+int lane_init(Lane& L, int priority = 0);
 void lane_free(Lane& L);
 int launch_programs(mps_ctx* c, Lane& L, ::mps_prog* const* progs, int n, bool per_gate);
 double program_cost(const ::mps_prog* p, const DevOp* ops, size_t n_ops, bool with_obs);

@@ -23,6 +23,9 @@ namespace gbmps {
 // a batch fills the GPU only with ~150 circuits; more lanes let the small
 // batches that steady arrivals produce run side by side instead of queueing.
 constexpr int kServeLanes = 16;
+// Workers of the wide lane: a wide split's cooperative launches use at most
+// one CTA per eight rows, so two requests of caps up to 512 run side by side.
+constexpr int kWideLanes = 2;
 // Per-lane host-mapped arena for fused requests: 16 B of flags plus
 // 2 (n_terms + 1) doubles each (848 B for a 50-term Hamiltonian).
 constexpr size_t kArenaBytes = 2u << 20;
@@ -257,11 +260,14 @@ static void serve_loop(mps_ctx* c) {
   }
 }
 
-// Wide requests: one at a time on the wide lane (host-driven splits),
-// admitted under the same HBM footprint budget as the batches.
-static void serve_wide_loop(mps_ctx* c) {
+// Wide requests: each wide worker takes one at a time (host-driven splits on
+// its own lane and workspace), admitted under the same HBM footprint budget
+// as the batches.
+static void serve_wide_loop(mps_ctx* c, int w) {
   cudaSetDevice(c->device);
   ServeState* S = c->serve;
+  Lane& lane = S->wide_lanes[w];
+  void** ws = &S->wide_ws[w];
   for (;;) {
     ServeReq* r = nullptr;
     {
@@ -279,17 +285,17 @@ static void serve_wide_loop(mps_ctx* c) {
       S->inflight_reqs += 1;
     }
     mps_prog* p = r->prog;
-    int rc = wide_run(c, S->wide_lane, p, &S->wide_ws);
+    int rc = wide_run(c, lane, p, ws);
     double energy = 0.0;
     std::vector<uint8_t> all;
     if (!rc && p->d_obs) {
       std::vector<double> res(2 * ((size_t)p->n_terms + 1));
-      rc = wide_expect(p, p->obs_codes.data(), p->n_terms + 1, res.data(), &S->wide_lane, &S->wide_ws);
+      rc = wide_expect(p, p->obs_codes.data(), p->n_terms + 1, res.data(), &lane, ws);
       if (!rc) energy = observable_value(p, res.data());
     }
     if (!rc && r->shots > 0) {
       all.resize((size_t)r->shots * p->n);
-      rc = wide_sample(p, r->shots, r->seed, all.data(), &S->wide_lane, &S->wide_ws);
+      rc = wide_sample(p, r->shots, r->seed, all.data(), &lane, ws);
     }
     if (!rc) rc = prog_check_err(p);
     {
@@ -323,7 +329,9 @@ int mps_serve_start(mps_ctx* c, int max_inflight) {
   S->batches.resize(kServeLanes);
   S->lane_busy.assign(kServeLanes, 0);
   for (int l = 0; l < kServeLanes; ++l) {
-    int rc = lane_init(S->lanes[l]);
+    // batch lanes at the highest stream priority: their CTAs go first when
+    // SMs free up between the wide lane's cooperative launches
+    int rc = lane_init(S->lanes[l], 1);
     if (rc) return rc;
     e = cudaEventCreateWithFlags(&S->batches[l].ev, cudaEventDisableTiming);
     if (e != cudaSuccess) return fail(MPS_ERR_CUDA, cudaGetErrorString(e));
@@ -332,12 +340,16 @@ int mps_serve_start(mps_ctx* c, int max_inflight) {
     if (e != cudaSuccess) return fail(MPS_ERR_OOM, cudaGetErrorString(e));
     S->batches[l].arena_cap = kArenaBytes;
   }
-  int rc = lane_init(S->wide_lane);
-  if (rc) return rc;
+  S->wide_lanes.resize(kWideLanes);
+  S->wide_ws.assign(kWideLanes, nullptr);
+  for (int w = 0; w < kWideLanes; ++w) {
+    const int rc = lane_init(S->wide_lanes[w], -1);
+    if (rc) return rc;
+  }
   S->running = true;
   c->serve = S;
   S->worker = std::thread(serve_loop, c);
-  S->wide_worker = std::thread(serve_wide_loop, c);
+  for (int w = 0; w < kWideLanes; ++w) S->wide_workers.emplace_back(serve_wide_loop, c, w);
   return MPS_OK;
 }
 
@@ -411,10 +423,11 @@ int mps_serve_stop(mps_ctx* c) {
   S->cv_work.notify_all();
   S->cv_wide.notify_all();
   if (S->worker.joinable()) S->worker.join();
-  if (S->wide_worker.joinable()) S->wide_worker.join();
+  for (std::thread& t : S->wide_workers)
+    if (t.joinable()) t.join();
   cudaSetDevice(c->device);
-  lane_free(S->wide_lane);
-  wide_ws_free(&S->wide_ws);
+  for (Lane& l : S->wide_lanes) lane_free(l);
+  for (void*& w : S->wide_ws) wide_ws_free(&w);
   for (int l = 0; l < kServeLanes; ++l) {
     lane_free(S->lanes[l]);
     if (S->batches[l].ev) cudaEventDestroy(S->batches[l].ev);
