@@ -343,18 +343,67 @@ __device__ void tridiagonalize(cx<T>* A, int m, double trace, SmallSmem<T>* sm) 
       const cx<T>* part = reinterpret_cast<const cx<T>*>(sm->red);
       for (int w = 0; w < (nt >> 5); ++w) d = d + part[w];
       const cx<T> a2 = scl(tau * d, T(-0.5));
-      for (int t = tid; t < L * L; t += nt) {
-        const int r = t / L, c = t - r * L;
-        const cx<T> vr = sm->tv[r], vc = sm->tv[c];
-        const cx<T> wr = sm->tp[r] + a2 * vr, wc = sm->tp[c] + a2 * vc;
-        cx<T>& a = A[(j + 1 + r) * lda + (j + 1 + c)];
-        a = a - (vr * conj(wc) + wr * conj(vc));
+      if (L >= 32) {
+        // a warp per row, lanes over its columns: no index division per
+        // element, and the row's v and w are loaded once (same arithmetic)
+        const int nw = nt >> 5;
+        for (int r = warp; r < L; r += nw) {
+          const cx<T> vr = sm->tv[r];
+          const cx<T> wr = sm->tp[r] + a2 * vr;
+          cx<T>* arow = A + (j + 1 + r) * lda + (j + 1);
+          for (int c = lane; c < L; c += 32) {
+            const cx<T> vc = sm->tv[c];
+            const cx<T> wc = sm->tp[c] + a2 * vc;
+            arow[c] = arow[c] - (vr * conj(wc) + wr * conj(vc));
+          }
+        }
+      } else {
+        for (int t = tid; t < L * L; t += nt) {
+          const int r = t / L, c = t - r * L;
+          const cx<T> vr = sm->tv[r], vc = sm->tv[c];
+          const cx<T> wr = sm->tp[r] + a2 * vr, wc = sm->tp[c] + a2 * vc;
+          cx<T>& a = A[(j + 1 + r) * lda + (j + 1 + c)];
+          a = a - (vr * conj(wc) + wr * conj(vc));
+        }
       }
     }
     __syncthreads();
   }
   for (int i = tid; i < m; i += nt) sm->td[i] = A[i * lda + i].re;
   __syncthreads();
+}
+
+// Number of eigenvalues below x of the unreduced block [s, t] of (td, te),
+// FP64, without a division per step.  The pivots q_i = (d_i - x) - e_{i-1}^2
+// / q_{i-1} of the usual count are ratios p_i / p_{i-1} of the leading
+// principal minors p_i = (d_i - x) p_{i-1} - e_{i-1}^2 p_{i-2}, so a negative
+// pivot is a sign change between consecutive minors.  A pivot below pivmin
+// in magnitude is set to -pivmin, as in the division form (p_i = -pivmin
+// p_{i-1}).  The pair (p_{i-1}, p_i) is rescaled by a power of two whenever
+// p_i leaves [2^-500, 2^500], which keeps the ratios exact.  FP64 division
+// is a long sequence on a pipe with 1/63 of the FP32 rate; this count uses
+// three multiply-adds per step.
+__device__ __forceinline__ int sturm_count_minors(const double* td, const double* te, int s, int t, double x,
+                                                  double pivmin) {
+  int cnt = 0;
+  double pm = 1.0, pc = td[s] - x;  // p_{i-1}, p_i
+  if (fabs(pc) < pivmin) pc = -pivmin;
+  cnt += pc < 0.0;
+  for (int i = s + 1; i <= t; ++i) {
+    const double e = te[i - 1];
+    double pn = fma(td[i] - x, pc, -(e * e) * pm);
+    if (fabs(pn) < pivmin * fabs(pc)) pn = -pivmin * pc;
+    cnt += (pn < 0.0) != (pc < 0.0);
+    pm = pc;
+    pc = pn;
+    const int ex = (__double2hiint(pc) >> 20) & 0x7ff;  // biased exponent of p_i
+    if (ex > 1023 + 500 || ex < 1023 - 500) {
+      const double sc = __hiloint2double((2046 - ex) << 20, 0);  // ~1 / |p_i|, a power of two
+      pc *= sc;
+      pm *= sc;
+    }
+  }
+  return cnt;
 }
 
 // All eigenvalues of T (td, te): split into unreduced blocks, then each row j
@@ -393,12 +442,16 @@ __device__ void tri_multisect(int m, SmallSmem<T>* sm, int rounds) {
     const T w = (b - a) / T(L + 1);
     const T x = a + w * T(q + 1);
     int cnt = 0;
-    T qv = T(1);
-    for (int i = s; i <= t; ++i) {
-      const T e2 = i > s ? sm->te[i - 1] * sm->te[i - 1] : T(0);
-      qv = (sm->td[i] - x) - (i > s ? e2 / qv : T(0));
-      if (fabs(qv) < pivmin) qv = -pivmin;
-      cnt += qv < T(0);
+    if constexpr (sizeof(T) == 8) {
+      cnt = sturm_count_minors(sm->td, sm->te, s, t, x, pivmin);
+    } else {
+      T qv = T(1);
+      for (int i = s; i <= t; ++i) {
+        const T e2 = i > s ? sm->te[i - 1] * sm->te[i - 1] : T(0);
+        qv = (sm->td[i] - x) - (i > s ? e2 / qv : T(0));
+        if (fabs(qv) < pivmin) qv = -pivmin;
+        cnt += qv < T(0);
+      }
     }
     // the new bracket ends at the first point whose count exceeds `local`
     int first = L;
@@ -530,10 +583,20 @@ __device__ void tri_backtransform(const cx<T>* A, cx<T>* W, int m, int k, int ld
       sm->twv[c] = tau * acc;
     }
     __syncthreads();
-    for (int t = tid; t < L * k; t += nt) {
-      const int i = t / k, c = t - i * k;
-      const cx<T> v = i == 0 ? mk<T>(1, 0) : A[(j + 1 + i) * lda + j];
-      W[(j + 1 + i) * ld + c] = W[(j + 1 + i) * ld + c] - v * sm->twv[c];
+    if (k >= 32) {
+      // a warp per row of W, lanes over its columns (no index division)
+      const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+      for (int i = warp; i < L; i += nw) {
+        const cx<T> v = i == 0 ? mk<T>(1, 0) : A[(j + 1 + i) * lda + j];
+        cx<T>* wrow = W + (j + 1 + i) * ld;
+        for (int c = lane; c < k; c += 32) wrow[c] = wrow[c] - v * sm->twv[c];
+      }
+    } else {
+      for (int t = tid; t < L * k; t += nt) {
+        const int i = t / k, c = t - i * k;
+        const cx<T> v = i == 0 ? mk<T>(1, 0) : A[(j + 1 + i) * lda + j];
+        W[(j + 1 + i) * ld + c] = W[(j + 1 + i) * ld + c] - v * sm->twv[c];
+      }
     }
     __syncthreads();
   }
