@@ -29,6 +29,11 @@ struct mps_graph {
   double* h_cycles = nullptr;
   std::vector<gbmps::ProgDesc> desc_of;
   std::vector<int> order;
+  // pinned staging of the op table for mps_graph_update (the host-to-device
+  // copy runs at full bus speed and asynchronously); copied_ev marks the end
+  // of the last copy out of it
+  gbmps::DevOp* h_ops = nullptr;
+  cudaEvent_t copied_ev = nullptr;
 };
 
 namespace gbmps {
@@ -69,6 +74,8 @@ int mps_graph_destroy(mps_graph* g) {
   if (g->graph) cudaGraphDestroy(g->graph);
   if (g->h_out) cudaFreeHost(g->h_out);
   if (g->h_cycles) cudaFreeHost(g->h_cycles);
+  if (g->h_ops) cudaFreeHost(g->h_ops);
+  if (g->copied_ev) cudaEventDestroy(g->copied_ev);
   if (g->d_cycles) cudaFree(g->d_cycles);
   for (int i = 0; i < 3; ++i)
     if (g->ev[i]) cudaEventDestroy(g->ev[i]);
@@ -212,9 +219,21 @@ int mps_graph_update(mps_graph* g) {
     if (flat[i].kind != g->flat[i].kind || flat[i].site != g->flat[i].site || flat[i].orient != g->flat[i].orient)
       return fail(MPS_ERR_ARG, "update changes the circuit structure");
   g->flat.swap(flat);
-  if (!g->flat.empty())
-    GCK(cudaMemcpyAsync(g->L.d_ops, g->flat.data(), g->flat.size() * sizeof(DevOp), cudaMemcpyHostToDevice,
-                        g->L.stream));
+  if (g->flat.empty()) return MPS_OK;
+  const size_t bytes = g->flat.size() * sizeof(DevOp);
+  if (!g->h_ops) {
+    if (cudaMallocHost(&g->h_ops, bytes) != cudaSuccess || cudaEventCreateWithFlags(&g->copied_ev,
+                                                                                    cudaEventDisableTiming) !=
+                                                                 cudaSuccess) {
+      cudaGetLastError();
+      return fail(MPS_ERR_OOM, "pinned op-table staging failed");
+    }
+  } else {
+    GCK(cudaEventSynchronize(g->copied_ev));  // the previous copy has left the staging buffer
+  }
+  std::memcpy(g->h_ops, g->flat.data(), bytes);
+  GCK(cudaMemcpyAsync(g->L.d_ops, g->h_ops, bytes, cudaMemcpyHostToDevice, g->L.stream));
+  GCK(cudaEventRecord(g->copied_ev, g->L.stream));
   return MPS_OK;
 }
 
