@@ -73,6 +73,9 @@ extern "C" {
                                pair into one split (no reference counterpart: the reference
                                splits after every routed SWAP; exact in exact arithmetic,
                                fewer truncations otherwise) */
+#define MPS_FLAG_DENSITY 16 /* noisy circuits: the program holds the density matrix rho of
+                               n_qubits qubits as a vectorised MPS on 2 * n_qubits sites (ket
+                               of qubit q on site 2q, bra on site 2q+1); see mps_channel1 */
 
 /* largest bond dimension the single-CTA gate kernel handles */
 #define MPS_CHI_LIMIT 64
@@ -81,6 +84,10 @@ extern "C" {
 #define MPS_WIDE_CHI_LIMIT 1024
 /* largest qubit count for mps_amplitudes */
 #define MPS_AMP_QUBITS_MAX 26
+/* largest selections of mps_density_matrix (4^k entries) and of
+ * mps_density_diag and density-program sampling (2^k entries) */
+#define MPS_DM_QUBITS_MAX 13
+#define MPS_DIAG_QUBITS_MAX 24
 
 typedef struct mps_ctx mps_ctx;
 typedef struct mps_prog mps_prog;
@@ -167,8 +174,32 @@ int mps_sample(mps_prog* p, int shots, uint64_t seed, uint8_t* bits);
 int mps_n_measured(mps_prog* p, int* out);
 /* product over 2-qubit gates of (1 - discarded weight fraction) */
 int mps_truncation_fidelity(mps_prog* p, double* out);
-int mps_bond_dims(mps_prog* p, int* out); /* n_qubits-1 ints */
+int mps_bond_dims(mps_prog* p, int* out); /* sites-1 ints (2*n_qubits-1 for density programs) */
 int mps_stats(mps_prog* p, double out[4]); /* fidelity, max discarded, #2q gates, #ops */
+
+/* Noisy circuits (programs begun with MPS_FLAG_DENSITY).  Replace the
+ * purified-MPS visitor exatn-pmps (visitors/exatn-mpo/ExaTnPmpsVisitor.cpp):
+ * its gates (:820-885) are recorded with the same calls as for a state
+ * (rho -> U rho U^H), and mps_channel1 replaces applyKrausOp /
+ * applyLocalKrausOp (:887-1130): rho -> sum_k K_k rho K_k^H on one qubit,
+ * kraus = n_kraus 2x2 matrices of interleaved (re, im) doubles, row-major
+ * (like the reference, channels act on one qubit; convertNoiseChannel
+ * :797-818 drops the others).  The results replace finalize (:658-795):
+ *   mps_density_matrix  rho reduced to the selected qubits (the others
+ *                       traced out), 2^k x 2^k complex, row-major, row =
+ *                       ket, bit a of an index = qubits[a]; not normalised
+ *                       (its trace is Tr rho); k <= MPS_DM_QUBITS_MAX
+ *   mps_density_diag    its diagonal (2^k doubles), k <= MPS_DIAG_QUBITS_MAX
+ *   mps_expect_pauli    Tr(rho P) / Tr(rho) per string (same arguments)
+ *   mps_norm            Tr(rho)
+ *   mps_sample          shots drawn from the diagonal of rho reduced to the
+ *                       measured qubits (readout errors are the caller's)
+ * State-only calls (amplitudes, attached observables, captured graphs, the
+ * serve loop) return MPS_ERR_UNSUPPORTED for density programs; channels on
+ * a state program return MPS_ERR_STATE. */
+int mps_channel1(mps_prog* p, int qubit, int n_kraus, const double* kraus);
+int mps_density_matrix(mps_prog* p, int n_sel, const int* qubits, double* out);
+int mps_density_diag(mps_prog* p, int n_sel, const int* qubits, double* out);
 
 /* Captured batch (CUDA graph).  mps_graph_create consumes the gates recorded
  * on each program and captures: reset to |0...0>, one persistent launch over

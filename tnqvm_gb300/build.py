@@ -13,7 +13,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT, "libgb300mps.so")
-SOURCES = ["k_ops.cu", "k_measure.cu", "engine.cu", "serve.cu", "graph.cu", "k_gemm.cu", "k_coop.cu", "wide.cu"]
+SOURCES = ["k_ops.cu", "k_measure.cu", "engine.cu", "serve.cu", "graph.cu", "k_gemm.cu", "k_coop.cu", "wide.cu", "density.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 

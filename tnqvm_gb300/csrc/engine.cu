@@ -699,6 +699,12 @@ int mps_program_begin(mps_ctx* c, int n, int chi_max, double cutoff, int trunc_m
     return fail(MPS_ERR_UNSUPPORTED, "the per-gate visitor path runs the single-CTA kernel (bond cap <= " +
                                          std::to_string(MPS_CHI_LIMIT) + ")");
   if (chi_max <= 0) chi_max = MPS_CHI_LIMIT;
+  // a density program holds vec(rho) of n qubits on 2n sites
+  const int nq = n;
+  if (flags & MPS_FLAG_DENSITY) {
+    if (n > (1 << 20)) return fail(MPS_ERR_ARG, "too many qubits");
+    n = 2 * n;
+  }
   if (precision == MPS_PREC_SPLIT_BF16) precision = MPS_PREC_FP32;  // complex64 storage
   if (precision == MPS_PREC_AUTO) {
     // complex128 where the register is small and exact at its cap
@@ -710,6 +716,8 @@ int mps_program_begin(mps_ctx* c, int n, int chi_max, double cutoff, int trunc_m
   mps_prog* p = new mps_prog();
   p->ctx = c;
   p->n = n;
+  p->nq = nq;
+  p->density = (flags & MPS_FLAG_DENSITY) != 0;
   p->chi_cap = chi_max;
   p->mode = trunc_mode;
   p->prec = precision;
@@ -786,8 +794,28 @@ int mps_program_destroy(mps_prog* p) {
 }
 
 static int check_q(mps_prog* p, int q) {
-  if (q < 0 || q >= p->n) return fail(MPS_ERR_ARG, "qubit index out of range");
+  if (q < 0 || q >= p->nq) return fail(MPS_ERR_ARG, "qubit index out of range");
   return MPS_OK;
+}
+
+// Record a gate on qubits; a density program applies U to the ket sites and
+// conj(U) to the bra sites: rho -> U rho U^H.
+static void push_gate(mps_prog* p, const GateRec& g) {
+  if (!p->density) {
+    p->pending.push_back(g);
+    return;
+  }
+  GateRec k = g, b = g;
+  k.q0 = 2 * g.q0;
+  b.q0 = 2 * g.q0 + 1;
+  if (g.nq == 2) {
+    k.q1 = 2 * g.q1;
+    b.q1 = 2 * g.q1 + 1;
+  }
+  const int ne = g.nq == 2 ? 16 : 4;
+  for (int i = 0; i < ne; ++i) b.m[i] = std::conj(g.m[i]);
+  p->pending.push_back(k);
+  p->pending.push_back(b);
 }
 
 int mps_gate1(mps_prog* p, int q, const double m[8]) {
@@ -798,7 +826,7 @@ int mps_gate1(mps_prog* p, int q, const double m[8]) {
   g.q0 = q;
   g.q1 = -1;
   for (int i = 0; i < 4; ++i) g.m[i] = cd(m[2 * i], m[2 * i + 1]);
-  p->pending.push_back(g);
+  push_gate(p, g);
   return MPS_OK;
 }
 
@@ -811,7 +839,7 @@ int mps_gate2(mps_prog* p, int q0, int q1, const double m[32]) {
   g.q0 = q0;
   g.q1 = q1;
   for (int i = 0; i < 16; ++i) g.m[i] = cd(m[2 * i], m[2 * i + 1]);
-  p->pending.push_back(g);
+  push_gate(p, g);
   return MPS_OK;
 }
 
@@ -843,7 +871,7 @@ int mps_gate_named(mps_prog* p, const char* name, const int* qubits, int nq, con
   g.q0 = qubits[0];
   g.q1 = k == 2 ? qubits[1] : -1;
   if (k == 2 && g.q0 == g.q1) return fail(MPS_ERR_ARG, "two-qubit gate on one qubit");
-  p->pending.push_back(g);
+  push_gate(p, g);
   return MPS_OK;
 }
 
@@ -903,10 +931,28 @@ int mps_expect_pauli(mps_prog* p, const char* paulis, int n_terms, const double*
   int rc = flush_pending(p);
   if (rc) return rc;
   std::vector<uint8_t> codes;
-  rc = parse_paulis(p->n, paulis, n_terms, codes);
+  rc = parse_paulis(p->nq, paulis, n_terms, codes);
   if (rc) return rc;
   if (n_terms == 0) {
     if (coeffs) out[0] = 0.0;
+    return MPS_OK;
+  }
+  if (p->density) {
+    // Tr(rho P) / Tr(rho) for every term in one walk of the doubled chain
+    std::vector<cx<double>> res;
+    rc = density_expect(p, codes.data(), n_terms, res);
+    if (rc) return rc;
+    const cx<double> tr = res[n_terms];
+    const double d = tr.re * tr.re + tr.im * tr.im;
+    if (!(d > 0.0)) return fail(MPS_ERR_NUMERIC, "density matrix with zero trace");
+    double e = 0.0;
+    for (int t = 0; t < n_terms; ++t) {
+      const cx<double> v = res[t];
+      out[2 * t] = (v.re * tr.re + v.im * tr.im) / d;
+      out[2 * t + 1] = (v.im * tr.re - v.re * tr.im) / d;
+      if (coeffs) e += coeffs[t] * out[2 * t];
+    }
+    if (coeffs) out[2 * n_terms] = e;
     return MPS_OK;
   }
   if (prog_is_wide(p)) {
@@ -956,6 +1002,19 @@ int mps_expect_pauli(mps_prog* p, const char* paulis, int n_terms, const double*
 
 int mps_norm(mps_prog* p, double* out) {
   if (!p || !out) return fail(MPS_ERR_ARG, "NULL argument");
+  if (p->density) {
+    // the trace of rho
+    mps_ctx* c = p->ctx;
+    std::lock_guard<std::mutex> lk(c->mu);
+    CK(cudaSetDevice(c->device));
+    int rc = flush_pending(p);
+    if (rc) return rc;
+    std::vector<cx<double>> res;
+    rc = density_expect(p, nullptr, 0, res);
+    if (rc) return rc;
+    *out = res[0].re;
+    return MPS_OK;
+  }
   std::string ids(p->n, 'I');
   double v[2];
   int rc = mps_expect_pauli(p, ids.c_str(), 1, nullptr, v);
@@ -966,6 +1025,8 @@ int mps_norm(mps_prog* p, double* out) {
 
 int mps_set_observable(mps_prog* p, const char* paulis, int n_terms, const double* coeffs) {
   if (!p || n_terms < 0 || (n_terms > 0 && (!paulis || !coeffs))) return fail(MPS_ERR_ARG, "NULL argument");
+  if (p->density)
+    return fail(MPS_ERR_UNSUPPORTED, "attached observables are for state programs; use mps_expect_pauli");
   std::vector<uint8_t> codes;
   int rc = parse_paulis(p->n, paulis, n_terms, codes);
   if (rc) return rc;
@@ -1025,6 +1086,7 @@ int mps_batch_expect(mps_ctx* c, mps_prog* const* progs, int n, double* out) {
 
 int mps_amplitudes(mps_prog* p, double* out) {
   if (!p || !out) return fail(MPS_ERR_ARG, "NULL argument");
+  if (p->density) return fail(MPS_ERR_UNSUPPORTED, "a density program has no state vector; use mps_density_matrix");
   if (p->n > MPS_AMP_QUBITS_MAX) return fail(MPS_ERR_UNSUPPORTED, "too many qubits for a full state vector");
   mps_ctx* c = p->ctx;
   std::lock_guard<std::mutex> lk(c->mu);
@@ -1065,6 +1127,7 @@ int mps_amplitudes(mps_prog* p, double* out) {
 
 int mps_amplitude(mps_prog* p, const int* bits, double out[2]) {
   if (!p || !bits || !out) return fail(MPS_ERR_ARG, "NULL argument");
+  if (p->density) return fail(MPS_ERR_UNSUPPORTED, "a density program has no state vector; use mps_density_matrix");
   for (int i = 0; i < p->n; ++i)
     if (bits[i] != 0 && bits[i] != 1) return fail(MPS_ERR_ARG, "bits must be 0 or 1");
   mps_ctx* c = p->ctx;
@@ -1092,7 +1155,7 @@ int mps_amplitude(mps_prog* p, const int* bits, double out[2]) {
 
 int mps_n_measured(mps_prog* p, int* out) {
   if (!p || !out) return fail(MPS_ERR_ARG, "NULL argument");
-  *out = p->measured.empty() ? p->n : (int)p->measured.size();
+  *out = p->measured.empty() ? p->nq : (int)p->measured.size();
   return MPS_OK;
 }
 
@@ -1104,6 +1167,7 @@ int mps_sample(mps_prog* p, int shots, uint64_t seed, uint8_t* bits) {
   CK(cudaSetDevice(c->device));
   int rc = flush_pending(p);
   if (rc) return rc;
+  if (p->density) return density_sample(p, shots, seed, bits);
   std::vector<uint8_t> all((size_t)shots * p->n);
   if (prog_is_wide(p))
     rc = wide_sample(p, shots, seed, all.data());

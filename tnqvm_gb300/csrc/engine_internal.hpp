@@ -140,6 +140,10 @@ struct mps_ctx {
 struct mps_prog {
   mps_ctx* ctx = nullptr;
   int n = 0, chi_cap = 0, mode = 0, prec = 0, flags = 0;
+  // qubits of the register: n for a state, n / 2 for a density program
+  // (MPS_FLAG_DENSITY: ket of qubit q on site 2q, bra on site 2q + 1)
+  int nq = 0;
+  bool density = false;
   int prec_mode = 0;        // the precision requested at begin (MPS_PREC_*), reported back
   bool split_bf16 = false;  // wide-path tensor-core products with bf16 hi/lo operands
   double cutoff = 0.0;
@@ -202,4 +206,7 @@ int wide_diag_cgemm_kind(mps_ctx* c, int prec, int kind, int flags, int M, int N
                          const double* b, double* out);
 int wide_gemm_tunings(mps_ctx* c);
 void wide_free(mps_ctx* c);
+// density programs (density.cu)
+int density_expect(::mps_prog* p, const uint8_t* codes, int n_terms, std::vector<cx<double>>& res);
+int density_sample(::mps_prog* p, int shots, uint64_t seed, uint8_t* bits);
 }  // namespace gbmps

@@ -91,6 +91,7 @@ int mps_graph_create(mps_ctx* c, mps_prog* const* progs, int n, mps_graph** out)
     if (!progs[i] || progs[i]->ctx != c) return fail(MPS_ERR_ARG, "program from another context");
     if (prog_is_wide(progs[i]))
       return fail(MPS_ERR_UNSUPPORTED, "captured batches hold single-CTA programs (bond cap <= 64)");
+    if (progs[i]->density) return fail(MPS_ERR_UNSUPPORTED, "captured batches hold state programs");
   }
   std::lock_guard<std::mutex> lk(c->mu);
   GCK(cudaSetDevice(c->device));

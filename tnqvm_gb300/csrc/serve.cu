@@ -357,6 +357,7 @@ int mps_serve_submit(mps_ctx* c, mps_prog* p, int shots, uint64_t seed, uint64_t
   if (!c || !p || !ticket || shots < 0) return fail(MPS_ERR_ARG, "bad argument");
   if (!c->serve) return fail(MPS_ERR_STATE, "serve loop not started");
   if (p->ctx != c) return fail(MPS_ERR_ARG, "program from another context");
+  if (p->density) return fail(MPS_ERR_UNSUPPORTED, "the serve loop runs state programs");
   ServeState* S = c->serve;
   ServeReq* r = new ServeReq();
   r->prog = p;

@@ -17,7 +17,8 @@ OK, ERR_ARG, ERR_OOM, ERR_TIMEOUT, ERR_NUMERIC, ERR_CUDA, ERR_STATE, ERR_UNSUPPO
 TRUNC_EXATN, TRUNC_ITENSOR = 0, 1
 PREC_FP64, PREC_FP32, PREC_AUTO, PREC_SPLIT_BF16 = 0, 1, 2, 3
 AUTO_FP64_QUBITS = 12
-FLAG_RENORM, FLAG_PER_GATE, FLAG_SWEEP, FLAG_FUSE = 1, 2, 4, 8
+FLAG_RENORM, FLAG_PER_GATE, FLAG_SWEEP, FLAG_FUSE, FLAG_DENSITY = 1, 2, 4, 8, 16
+DM_QUBITS_MAX, DIAG_QUBITS_MAX = 13, 24
 CHI_LIMIT = 64
 WIDE_CHI_LIMIT = 1024
 # GEMM kernels of the wide path (MPS_GEMM_*) and the autotuner's row width
@@ -92,6 +93,9 @@ SIGNATURES = [
     ("mps_autotune_load", _c.c_int, [_c.c_char_p]),
     ("mps_autotune_clear", _c.c_int, []),
     ("mps_autotune_tunings", _c.c_int, [_P, _c.POINTER(_c.c_int)]),
+    ("mps_channel1", _c.c_int, [_P, _c.c_int, _c.c_int, _DP]),
+    ("mps_density_matrix", _c.c_int, [_P, _c.c_int, _c.POINTER(_c.c_int), _DP]),
+    ("mps_density_diag", _c.c_int, [_P, _c.c_int, _c.POINTER(_c.c_int), _DP]),
 ]
 
 GATE_IDS = {name: i for i, name in enumerate(
@@ -507,6 +511,45 @@ class Program:
         out = (ctypes.c_int * max(self.n - 1, 1))()
         _check(_lib.mps_bond_dims(self.h, out))
         return list(out)[: self.n - 1]
+
+    # ---- noisy circuits (DensityProgram)
+    def channel(self, q, kraus):
+        """rho -> sum_k K_k rho K_k^H on qubit q (density programs)."""
+        k = np.ascontiguousarray(np.asarray(kraus, dtype=np.complex128).reshape(-1, 2, 2))
+        _check(_lib.mps_channel1(self.h, q, k.shape[0], _dptr(k.view(np.float64).reshape(-1))))
+
+    def density_matrix(self, qubits):
+        """rho reduced to ``qubits`` (bit a of an index = qubits[a]), not normalised."""
+        qubits = list(qubits)
+        k = len(qubits)
+        out = np.zeros(2 << (2 * k), dtype=np.float64)
+        q = (ctypes.c_int * k)(*qubits)
+        _check(_lib.mps_density_matrix(self.h, k, q, _dptr(out)))
+        return out.view(np.complex128).reshape(1 << k, 1 << k)
+
+    def density_diag(self, qubits):
+        qubits = list(qubits)
+        k = len(qubits)
+        out = np.zeros(1 << k, dtype=np.float64)
+        q = (ctypes.c_int * k)(*qubits)
+        _check(_lib.mps_density_diag(self.h, k, q, _dptr(out)))
+        return out
+
+
+class DensityProgram(Program):
+    """Noisy circuit: the density matrix of ``n`` qubits as a vectorised MPS
+    on 2n sites (MPS_FLAG_DENSITY).  Gates act as rho -> U rho U^H, ``channel``
+    applies Kraus channels; ``bond_dims`` lists the 2n-1 bonds of the doubled
+    chain."""
+
+    def __init__(self, ctx, n, chi_max=0, cutoff=-1.0, mode=TRUNC_EXATN, precision=PREC_FP64, flags=0):
+        super().__init__(ctx, n, chi_max, cutoff, mode, precision, flags | FLAG_DENSITY)
+
+    def bond_dims(self):
+        m = 2 * self.n
+        out = (ctypes.c_int * (m - 1))()
+        _check(_lib.mps_bond_dims(self.h, out))
+        return list(out)
 
     def stats(self):
         out = np.zeros(4)

@@ -233,3 +233,145 @@ class GpuMpsVisitor:
             return 0.0
         v = self.prog.expect_pauli(["".join(letters)])[0]
         return sign * float(v.real)
+
+
+MAX_QUBITS_FOR_DENSITY_MATRIX = M.DM_QUBITS_MAX   # the reference's bound is 15 (ExaTnPmpsVisitor.cpp:662)
+
+
+class GpuPmpsVisitor:
+    """``tnqvm-visitor`` name ``gb300-pmps``: noisy circuits, the drop-in for
+    the purified-MPS visitor ``exatn-pmps``
+    (``visitors/exatn-mpo/ExaTnPmpsVisitor.cpp``).  The density matrix is held
+    as a vectorised MPS on the GPU (``DensityProgram``); each gate is followed
+    by the single-qubit Kraus channels the noise model gives for it
+    (``applySingleQubitGate`` / ``applyTwoQubitGate`` ``:820-885``).
+
+    Options: ``noise-model`` (a ``JsonNoiseModel``, any object with its two
+    methods, or the JSON text), ``backend-json`` (JSON text of the same
+    format; the reference reads an IBM backend description there, which
+    needs XACC's IBM noise model), ``shots`` (default 1024, ``:539``),
+    ``seed``, ``max-bond-dim``, ``svd-cutoff``, ``precision``,
+    ``truncation-mode``."""
+
+    def __init__(self, ctx=None):
+        self.ctx = ctx
+        self.options = {}
+        self.prog = None
+        self.buffer = None
+        self.noise = None
+        self.measured = []
+        self.shots = 1024
+
+    def name(self):
+        return "gb300-pmps"
+
+    def description(self):
+        return "Noisy-circuit simulator (density matrix as a vectorised MPS) on one GB300 GPU"
+
+    def clone(self):
+        v = GpuPmpsVisitor(self.ctx)
+        v.options = dict(self.options)
+        return v
+
+    def supportVqeMode(self):
+        return False
+
+    def setOptions(self, options):
+        self.options = dict(options)
+
+    def initialize(self, buffer, nbShots=1):
+        """ExaTnPmpsVisitor::initialize (:482-542)."""
+        from .noise import JsonNoiseModel
+        if self.ctx is None:
+            self.ctx = default_context()
+        o = self.options
+        nm = o.get("noise-model", o.get("backend-json"))
+        if isinstance(nm, (str, bytes)):
+            nm = JsonNoiseModel(nm)
+        self.noise = nm
+        mode = {"exatn": M.TRUNC_EXATN, "itensor": M.TRUNC_ITENSOR}[o.get("truncation-mode", "exatn")]
+        prec = {"fp64": M.PREC_FP64, "fp32": M.PREC_FP32}[o.get("precision", "fp64")]
+        cutoff = float(o["svd-cutoff"]) if "svd-cutoff" in o else -1.0
+        chi = int(o["max-bond-dim"]) if "max-bond-dim" in o else 0
+        if self.prog is not None:
+            self.prog.close()
+        self.buffer = buffer
+        # a noisy simulation always runs shots (:539)
+        self.shots = 1024 if nbShots < 1 else nbShots
+        self.prog = M.DensityProgram(self.ctx, buffer.size(), chi, cutoff, mode, prec)
+        self.measured = []
+
+    def visit(self, name, qubits, params=()):
+        if name == "Measure":
+            self.measured.append(qubits[0])
+            self.prog.measure(qubits[0])
+            return
+        self.prog.gate(name, list(qubits), list(params))
+        if self.noise is None:
+            return
+        for cq, mats in self.noise.channels(name, list(qubits)):
+            # single-qubit channels only (convertNoiseChannel :797-818)
+            if len(cq) == 1 and np.asarray(mats[0]).shape == (2, 2):
+                self.prog.channel(cq[0], mats)
+
+    def run(self, circuit):
+        for name, qs, ps in circuit:
+            self.visit(name, qs, ps)
+
+    def finalize(self):
+        """ExaTnPmpsVisitor::finalize (:658-795): the density matrix of the
+        register (or, for larger registers, of the measured qubits) as
+        ``density_matrix`` (row-major (re, im) pairs, row = ket, bit a of an
+        index = qubit a of the selection), then the shots drawn from its
+        diagonal with each measured bit flipped by the readout error."""
+        p, buf = self.prog, self.buffer
+        n = buf.size()
+        p.submit()
+        p.wait()
+        if not self.measured:
+            return
+        meas = list(self.measured)
+        if n <= MAX_QUBITS_FOR_DENSITY_MATRIX:
+            sel = list(range(n))
+        elif len(set(meas)) <= MAX_QUBITS_FOR_DENSITY_MATRIX:
+            sel = sorted(set(meas))
+        else:
+            raise ValueError("Measure more than %d is not supported." % MAX_QUBITS_FOR_DENSITY_MATRIX)
+        dm = p.density_matrix(sel)
+        buf.addExtraInfo("density_matrix", [(float(z.real), float(z.imag)) for z in dm.reshape(-1)])
+        seed = int(self.options.get("seed", np.random.SeedSequence().entropy % (1 << 63)))
+        bits = p.sample(self.shots, seed)
+        if self.noise is not None:
+            rng = np.random.default_rng(seed ^ 0x5EED)
+            u = rng.random(bits.shape)
+            for a, q in enumerate(meas):
+                m0p1, m1p0 = self.noise.readout_error(q)
+                flip = np.where(bits[:, a] == 1, m0p1, m1p0)
+                bits[:, a] ^= (u[:, a] < flip).astype(np.uint8)
+        keys = ["".join(map(str, row)) for row in bits]
+        for k, v in Counter(keys).items():
+            buf.appendMeasurement(k, v)
+        self.measured = []
+
+    def getExpectationValueZ(self, observed_circuit):
+        """<Z...Z> on the measured qubits of ``observed_circuit`` after its
+        basis change, as Tr(rho P) / Tr(rho) (the reference returns 0 here,
+        :1233-1236)."""
+        n = self.buffer.size()
+        letters = ["I"] * n
+        pending = {}
+        sign = 1.0
+        for name, qs, ps in observed_circuit:
+            if name == "Measure":
+                letter, s = pending.get(qs[0], ("Z", 1.0))
+                letters[qs[0]] = letter
+                sign *= s
+            elif name == "H":
+                pending[qs[0]] = ("X", 1.0)
+            elif name == "Rx" and abs(abs(ps[0]) - np.pi / 2) < 1e-12:
+                pending[qs[0]] = ("Y", 1.0 if ps[0] > 0 else -1.0)
+            else:
+                raise ValueError("unsupported basis-change gate %s" % name)
+        if all(c == "I" for c in letters):
+            return 0.0
+        return sign * float(self.prog.expect_pauli(["".join(letters)])[0].real)
