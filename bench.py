@@ -420,6 +420,7 @@ def extra_measurements(args, ctx, insts, energies, value, world):
                          "per_circuit_ms": 1e3 * dt / max(1, done),
                          "batched_over_plain": value / plain,
                          "max_abs_dE_vs_oracle": float(max(perr)) if perr else None}
+    out["plain_fp64_exatn"] = plain_exatn(args, ctx, [insts[i] for i in pidx[:done]], value)
     # serving latency: Poisson arrivals into the continuous-batching loop
     out["latency"] = serve_latency(args, ctx, insts, value)
     # one large circuit on the wide path, and the mixed-cap serving stream
@@ -427,6 +428,34 @@ def extra_measurements(args, ctx, insts, energies, value, world):
         out["wide_48q_chi512"] = wide_single(args, ctx)
     if args.serve_stream > 0:
         out["serve_stream"] = serve_stream(args, ctx)
+    return out
+
+
+def plain_exatn(args, ctx, sample, value):
+    """The per-circuit FP64 path in exatn semantics (the drop-in for the
+    exatn-mps visitor and the plugin's default): one launch per gate, and the
+    site-parallel single launch (MPS_FLAG_PARALLEL: the two-site updates of
+    one circuit on disjoint sites run on different SMs), against the
+    exatn-mode oracle on the same circuits, whose single-core time per
+    circuit is the CPU figure beside them."""
+    from tnqvm_gb300 import mps as M
+    from oracle.pool import OraclePool
+    with OraclePool(workers=1) as pool:
+        ref, wall, busy = pool.energies(sample, CHI, CUTOFF, mode="exatn")
+    out = {"sample": len(sample), "cpu_one_core_ms_per_circuit": 1e3 * busy / max(1, len(sample)),
+           "cpu": "numpy complex128 MPS with LAPACK SVD (exatn-mode oracle), one process, single-threaded BLAS"}
+    for key, flags in (("per_gate", M.FLAG_PER_GATE), ("parallel", M.FLAG_PARALLEL)):
+        errs = []
+        t0 = time.perf_counter()
+        for it, r in zip(sample, ref):
+            p = M.Program(ctx, it["n"], CHI, CUTOFF, M.TRUNC_EXATN, M.PREC_FP64, flags)
+            p.run(it["circuit"])
+            e = p.expect_pauli(it["paulis"], it["coeffs"])[1] / p.norm()
+            p.close()
+            errs.append(abs(e - r))
+        dt = time.perf_counter() - t0
+        out[key] = {"value": len(sample) / dt, "unit": UNIT, "per_circuit_ms": 1e3 * dt / max(1, len(sample)),
+                    "max_abs_dE_vs_oracle": float(max(errs)), "batched_over_this": value / (len(sample) / dt)}
     return out
 
 

@@ -76,6 +76,13 @@ extern "C" {
 #define MPS_FLAG_DENSITY 16 /* noisy circuits: the program holds the density matrix rho of
                                n_qubits qubits as a vectorised MPS on 2 * n_qubits sites (ket
                                of qubit q on site 2q, bra on site 2q+1); see mps_channel1 */
+#define MPS_FLAG_PARALLEL 32 /* a program submitted alone (mps_submit) runs its two-site updates
+                               on disjoint sites on different SMs at once, in one launch;
+                               each update computes what it computes in program order, so
+                               results are unchanged.  Exatn semantics (no centre moves)
+                               leaves many updates independent; itensor semantics chains
+                               them through the orthogonality centre.  No counterpart in
+                               the reference. */
 
 /* largest bond dimension the single-CTA gate kernel handles */
 #define MPS_CHI_LIMIT 64

@@ -95,8 +95,11 @@ def exatn_keep(s, cutoff, max_bond):
 
 
 class MPS:
-    def __init__(self, n, mode="exatn", chi_max=None, cutoff=None, renorm=False):
+    def __init__(self, n, mode="exatn", chi_max=None, cutoff=None, renorm=False, svd=None):
+        """``svd``: the SVD routine (default numpy's LAPACK gesdd); another
+        driver measures how sensitive a run is to the SVD's rounding."""
         assert mode in ("exatn", "itensor")
+        self.svd = np.linalg.svd if svd is None else svd
         self.n = n
         self.mode = mode
         if mode == "exatn":
@@ -162,7 +165,7 @@ class MPS:
         th, dl, dr = self.theta(lo, msite)
         if self.mode == "exatn":
             th = np.where(np.abs(th) < 1e-100, 0.0, th)
-        u, s, vh = np.linalg.svd(th, full_matrices=False)
+        u, s, vh = self.svd(th, full_matrices=False)
         total = float(np.sum(s ** 2))
         if self.mode == "exatn":
             k = exatn_keep(s, self.cutoff, self.chi_max)

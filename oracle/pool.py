@@ -14,12 +14,13 @@ _BLAS_ENV = ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS")
 
 
 def _energy_task(task):
-    """<H>/<psi|psi> of one circuit, itensor semantics, and the seconds it took."""
+    """<H>/<psi|psi> of one circuit in the given truncation semantics, and the
+    seconds it took."""
     from . import mps as omps
     from . import routing
-    n, circuit, paulis, coeffs, chi, cutoff = task
+    n, circuit, paulis, coeffs, chi, cutoff, mode = task
     t0 = time.perf_counter()
-    m = omps.run(n, routing.route(circuit), mode="itensor", chi_max=chi, cutoff=cutoff)
+    m = omps.run(n, routing.route(circuit), mode=mode, chi_max=chi, cutoff=cutoff)
     e = sum(c * m.expect_pauli(s).real for s, c in zip(paulis, coeffs)) / m.norm2()
     return float(e), time.perf_counter() - t0
 
@@ -43,13 +44,13 @@ class OraclePool:
         # import the oracle in every worker before any timing
         self.pool.map(_warm, range(self.workers))
 
-    def energies(self, insts, chi, cutoff):
+    def energies(self, insts, chi, cutoff, mode="itensor"):
         """Energies of ``insts`` (dicts with n, circuit, paulis, coeffs), in
         order, costliest first to balance the workers; returns (energies,
         wall seconds, summed worker seconds)."""
         order = sorted(range(len(insts)), key=lambda i: -insts[i]["n"] * len(insts[i]["circuit"]))
         tasks = [(insts[i]["n"], insts[i]["circuit"], list(insts[i]["paulis"]), list(insts[i]["coeffs"]), chi,
-                  cutoff) for i in order]
+                  cutoff, mode) for i in order]
         t0 = time.perf_counter()
         res = self.pool.map(_energy_task, tasks, chunksize=1)
         wall = time.perf_counter() - t0

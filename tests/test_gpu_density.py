@@ -65,20 +65,37 @@ def test_density_exact_vs_dense_oracle(ctx, mode, prec, tol):
 @pytest.mark.parametrize("mode,name", [(M.TRUNC_EXATN, "exatn"), (M.TRUNC_ITENSOR, "itensor")])
 def test_density_truncated_vs_doubled_chain_oracle(ctx, mode, name):
     """6 qubits (12 sites) at bond cap 8: the engine's truncations of vec(rho)
-    against the MPS oracle run on the same doubled chain, same semantics."""
+    against the MPS oracle run on the same doubled chain, same semantics.
+
+    Tolerance: 1e-10, or ten times the oracle's own spread between two
+    LAPACK SVD drivers (gesdd, gesvd) where that is larger.  In exatn
+    semantics the state is never brought to canonical form and both sites
+    keep sqrt(S): the next truncation sees the individual singular vectors,
+    not just the kept subspace, and on this noisy chain that makes the run
+    ill-conditioned (the two drivers differ by ~3e-7, a 1e-15 relative
+    perturbation of every theta moves the result by ~6e-7).  The itensor run
+    (canonical form, the state depends on the kept subspace only) agrees with
+    both drivers to 1e-15."""
+    import scipy.linalg as SL
     rng = np.random.default_rng(33)
     n = 6
     circ = _random_circuit(n, 6, rng)
     cutoff = 1e-12
     ref = run_doubled_mps(n, circ, name, 8, cutoff)
     rho_ref = vec_to_rho(ref.amplitudes(), n)
+    alt = run_doubled_mps(n, circ, name, 8, cutoff,
+                          svd=lambda t, full_matrices=False: SL.svd(t, full_matrices=False, lapack_driver="gesvd"))
+    spread = float(np.max(np.abs(vec_to_rho(alt.amplitudes(), n) - rho_ref)))
+    tol = max(1e-10, 10.0 * spread)
+    if mode == M.TRUNC_ITENSOR:
+        assert spread < 1e-13
     with M.DensityProgram(ctx, n, 8, cutoff, mode, M.PREC_FP64) as p:
         record(p, circ)
         p.submit()
         p.wait()
         assert p.bond_dims() == ref.bond_dims()
-        assert np.max(np.abs(p.density_matrix(range(n)) - rho_ref)) < 1e-10
-        assert abs(p.norm() - np.trace(rho_ref).real) < 1e-10
+        assert np.max(np.abs(p.density_matrix(range(n)) - rho_ref)) < tol
+        assert abs(p.norm() - np.trace(rho_ref).real) < tol
 
 
 def test_density_sampling_chi_square(ctx):

@@ -168,10 +168,10 @@ def run_doubled_dense(n, circuit, noise=None):
     return vec_to_rho(v, n)
 
 
-def run_doubled_mps(n, circuit, mode, chi, cutoff, noise=None):
+def run_doubled_mps(n, circuit, mode, chi, cutoff, noise=None, svd=None):
     """The MPS oracle on the doubled chain, long-range pairs routed as the
     engine routes them (NearestNeighborTransform order)."""
-    mps = MO.MPS(2 * n, mode, chi, cutoff)
+    mps = MO.MPS(2 * n, mode, chi, cutoff, svd=svd)
     for _, qs, m in doubled_ops(circuit, noise):
         if len(qs) == 1:
             mps.gate1(qs[0], m)

@@ -285,6 +285,7 @@ void lane_free(Lane& L) {
   if (L.d_exp_out) cudaFree(L.d_exp_out);
   if (L.d_work) cudaFree(L.d_work);
   if (L.d_queue) cudaFree(L.d_queue);
+  if (L.d_dag) cudaFree(L.d_dag);
   cudaStreamDestroy(L.stream);
   L = Lane();
 }
@@ -430,6 +431,30 @@ int launch_programs(mps_ctx* c, Lane& L, mps_prog* const* progs_in, int n_in, bo
         e = launch_ops(L.d_desc + i, 1, 1, nullptr, L.op_scratch, L.stream);
         if (e != cudaSuccess) return fail(MPS_ERR_CUDA, cudaGetErrorString(e));
       }
+    } else if (n == 1 && nd == 1 && (progs[0]->flags & MPS_FLAG_PARALLEL) && progs[0]->serve_flag == nullptr &&
+               flat.size() > 1) {
+      // site-parallel: per op, the number of earlier ops on each of its sites
+      const mps_prog* p = progs[0];
+      const size_t nops = flat.size();
+      std::vector<int> host((nops * 2) + 1 + p->n, 0);
+      std::vector<int> seen(p->n, 0);
+      for (size_t o = 0; o < nops; ++o) {
+        const DevOp& op = flat[o];
+        const int s0 = op.kind == OP_MOVE_L ? op.site - 1 : op.site;
+        host[2 * o] = seen[s0]++;
+        host[2 * o + 1] = op.kind == OP_GATE1 ? -1 : seen[s0 + 1]++;
+      }
+      const int width = std::max(1, p->n / 2);  // two-site ops that can run at once
+      rc = grow(&L.d_dag, &L.d_dag_cap, host.size());
+      if (rc) return rc;
+      e = cudaMemcpyAsync(L.d_dag, host.data(), host.size() * sizeof(int), cudaMemcpyHostToDevice, L.stream);
+      if (e != cudaSuccess) return fail(MPS_ERR_CUDA, cudaGetErrorString(e));
+      const int grid = std::min<int>({(int)nops, c->num_sms, width});
+      rc = ensure_bytes(&L.op_scratch, &L.op_scratch_ctas, c->num_sms, op_scratch_bytes());
+      if (rc) return rc;
+      e = launch_ops_sites(L.d_desc, reinterpret_cast<const int2*>(L.d_dag), L.d_dag + 2 * nops, grid,
+                           L.op_scratch, L.stream);
+      if (e != cudaSuccess) return fail(MPS_ERR_CUDA, cudaGetErrorString(e));
     } else {
       const int grid = std::min(nd, c->num_sms);
       rc = ensure_bytes(&L.op_scratch, &L.op_scratch_ctas, c->num_sms, op_scratch_bytes());
@@ -454,6 +479,7 @@ int prog_check_err(mps_prog* p) {
   if (e != cudaSuccess) return fail(MPS_ERR_CUDA, cudaGetErrorString(e));
   if (herr & ERR_NAN) return fail(MPS_ERR_NUMERIC, "non-finite value in a two-site split");
   if (herr & ERR_DIMS) return fail(MPS_ERR_UNSUPPORTED, "bond dimension beyond the kernel limit");
+  if (herr & ERR_TIMEOUT) return fail(MPS_ERR_TIMEOUT, "a site-parallel update waited past its bound");
   return MPS_OK;
 }
 

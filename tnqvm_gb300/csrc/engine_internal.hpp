@@ -19,6 +19,8 @@ size_t op_scratch_bytes();
 size_t op_smem_bytes();
 cudaError_t launch_ops(const ProgDesc* d_progs, int n_progs, int grid, int* d_queue, char* scratch,
                        cudaStream_t st);
+cudaError_t launch_ops_sites(const ProgDesc* d_prog, const int2* d_deps, int* d_ctr, int grid, char* scratch,
+                             cudaStream_t st);
 cudaError_t configure_ops();
 cudaError_t configure_expect();
 cudaError_t launch_reset(const ProgDesc* d_progs, int n_progs, cudaStream_t st);
@@ -53,6 +55,8 @@ struct Lane {
   char* d_work = nullptr;  // sampler environments, bits, offsets
   size_t d_work_cap = 0;
   int* d_queue = nullptr;
+  int* d_dag = nullptr;  // site-parallel runs: per-op dependencies, op counter, per-site counts
+  size_t d_dag_cap = 0;
   // pinned host staging
   DevOp* h_ops = nullptr;
   size_t h_ops_cap = 0;

@@ -29,6 +29,20 @@
 
 namespace gbmps {
 
+// Program statistics are updated by one thread per op.  Atomics, because a
+// program run site-parallel (k_run_ops_sites) has ops of several CTAs in
+// flight; in a sequential run the order of the additions is unchanged.
+__device__ __forceinline__ void stat_add(double* slot, double v) { atomicAdd(slot, v); }
+__device__ __forceinline__ void stat_max(double* slot, double v) {
+  unsigned long long* a = reinterpret_cast<unsigned long long*>(slot);
+  unsigned long long old = *(volatile unsigned long long*)a;
+  while (__longlong_as_double((long long)old) < v) {
+    const unsigned long long prev = atomicCAS(a, old, (unsigned long long)__double_as_longlong(v));
+    if (prev == old) break;
+    old = prev;
+  }
+}
+
 template <typename T>
 struct Prec;
 // u_in_smem: the m x m work matrix of the eigensolver (and the staged X)
@@ -1043,16 +1057,16 @@ __device__ void op_gate2(const ProgDesc& P, const DevOp& op, char* big, SmallSme
     if ((P.flags & 1) && kept > 0.0) rn = sqrt(total / kept);
     sm->ival[2] = k;
     sm->dval[2] = rn;
-    P.stats[ST_LOG_FID] += log1p(-(frac < 1.0 ? frac : 0.0));
-    if (frac > P.stats[ST_MAX_DISC]) P.stats[ST_MAX_DISC] = frac;
-    P.stats[ST_N_GATE2] += 1.0;
+    stat_add(P.stats + ST_LOG_FID, log1p(-(frac < 1.0 ? frac : 0.0)));
+    stat_max(P.stats + ST_MAX_DISC, frac);
+    stat_add(P.stats + ST_N_GATE2, 1.0);
     // algorithmic flops (complex MAC = 8): merge, gate, Gram, split
-    P.stats[ST_FLOPS] += 32.0 * dl * dm * dr + 128.0 * dl * dr + 8.0 * m * m * nn + 8.0 * k * nn * m +
-                         16.0 * m * k * k + refine_flops +
-                         (Prec<T>::refine && k < m ? 16.0 * m * nn * k + 16.0 * m * k * k : 0.0);
+    stat_add(P.stats + ST_FLOPS, 32.0 * dl * dm * dr + 128.0 * dl * dr + 8.0 * m * m * nn + 8.0 * k * nn * m +
+                                     16.0 * m * k * k + refine_flops +
+                                     (Prec<T>::refine && k < m ? 16.0 * m * nn * k + 16.0 * m * k * k : 0.0));
     // Householder tridiagonalisation (complex, both sides) and the back-transform
-    P.stats[ST_EIG_FLOPS] += (32.0 / 3.0) * m * m * m * (refine_flops > 0.0 ? 2.0 : 1.0) + 8.0 * m * m * k;
-    if (refine_flops > 0.0) P.stats[ST_N_REFINE] += 1.0;
+    stat_add(P.stats + ST_EIG_FLOPS, (32.0 / 3.0) * m * m * m * (refine_flops > 0.0 ? 2.0 : 1.0) + 8.0 * m * m * k);
+    if (refine_flops > 0.0) stat_add(P.stats + ST_N_REFINE, 1.0);
     if (bad) atomicOr(P.err, ERR_NAN);
   }
   __syncthreads();
@@ -1222,14 +1236,14 @@ __device__ void op_gate2(const ProgDesc& P, const DevOp& op, char* big, SmallSme
   if (tid == 0) {
     P.bond[lo + 1] = k;
     const long long c_end = clock64();
-    P.stats[ST_CYC_THETA] += (double)(c_theta - c_start);
-    P.stats[ST_CYC_GRAM] += (double)(c_gram - c_theta);
-    P.stats[ST_CYC_EIG] += (double)(c_eig - c_gram);
-    P.stats[ST_CYC_SPLIT] += (double)(c_end - c_eig);
-    P.stats[ST_CYC_TRID] += (double)cyc_trid;
-    P.stats[ST_CYC_BISECT] += (double)cyc_bisect;
-    P.stats[ST_CYC_VEC] += (double)cyc_vec;
-    P.stats[ST_CYC_ORTH] += (double)cyc_orth;
+    stat_add(P.stats + ST_CYC_THETA, (double)(c_theta - c_start));
+    stat_add(P.stats + ST_CYC_GRAM, (double)(c_gram - c_theta));
+    stat_add(P.stats + ST_CYC_EIG, (double)(c_eig - c_gram));
+    stat_add(P.stats + ST_CYC_SPLIT, (double)(c_end - c_eig));
+    stat_add(P.stats + ST_CYC_TRID, (double)cyc_trid);
+    stat_add(P.stats + ST_CYC_BISECT, (double)cyc_bisect);
+    stat_add(P.stats + ST_CYC_VEC, (double)cyc_vec);
+    stat_add(P.stats + ST_CYC_ORTH, (double)cyc_orth);
   }
 }
 
@@ -1274,9 +1288,9 @@ __device__ void op_move_r(const ProgDesc& P, const DevOp& op, char* big, SmallSm
   __syncthreads();
   if (tid == 0) {
     P.bond[c + 1] = k;
-    P.stats[ST_FLOPS] += 4.0 * k * nc * w;
-    P.stats[ST_EIG_FLOPS] += 32.0 * mr * nc * nc;
-    P.stats[ST_CYC_MOVE] += (double)(clock64() - c_start);
+    stat_add(P.stats + ST_FLOPS, 4.0 * k * nc * w);
+    stat_add(P.stats + ST_EIG_FLOPS, 32.0 * mr * nc * nc);
+    stat_add(P.stats + ST_CYC_MOVE, (double)(clock64() - c_start));
   }
 }
 
@@ -1321,9 +1335,9 @@ __device__ void op_move_l(const ProgDesc& P, const DevOp& op, char* big, SmallSm
   __syncthreads();
   if (tid == 0) {
     P.bond[c] = k;
-    P.stats[ST_FLOPS] += 4.0 * k * nc * h;
-    P.stats[ST_EIG_FLOPS] += 32.0 * mr * nc * nc;
-    P.stats[ST_CYC_MOVE] += (double)(clock64() - c_start);
+    stat_add(P.stats + ST_FLOPS, 4.0 * k * nc * h);
+    stat_add(P.stats + ST_EIG_FLOPS, 32.0 * mr * nc * nc);
+    stat_add(P.stats + ST_CYC_MOVE, (double)(clock64() - c_start));
   }
 }
 
@@ -1354,7 +1368,7 @@ __device__ void run_program(const ProgDesc& P, char* smem, char* scratch) {
     }
     __syncthreads();
   }
-  if (threadIdx.x == 0) P.stats[ST_N_OPS] += (double)P.n_ops;
+  if (threadIdx.x == 0) stat_add(P.stats + ST_N_OPS, (double)P.n_ops);
   if (P.n_obs > 0) {
     // the program's observables on this CTA (the shared memory of the
     // update is free now): per-request completion for the serve loop
@@ -1375,7 +1389,7 @@ __device__ void run_program(const ProgDesc& P, char* smem, char* scratch) {
       tk.codes = P.obs_codes + (size_t)t * P.n;
       expect_sweep<T>(tk, E, As, X, P.obs_out + 2 * t);
     }
-    if (threadIdx.x == 0) P.stats[ST_CYC_OBS] += (double)(clock64() - c_obs);
+    if (threadIdx.x == 0) stat_add(P.stats + ST_CYC_OBS, (double)(clock64() - c_obs));
   }
   if (P.cycles_out != nullptr && threadIdx.x == 0) *P.cycles_out = (double)(clock64() - c_begin);
   if (P.done != nullptr) {
@@ -1392,6 +1406,32 @@ __device__ void run_program(const ProgDesc& P, char* smem, char* scratch) {
 // spills) stays out of the complex64 body's.
 __device__ __noinline__ void run_program_f64(const ProgDesc& P, char* smem, char* scratch) {
   run_program<double>(P, smem, scratch);
+}
+
+// One op of a program on this CTA.
+template <typename T>
+__device__ void run_one_op(const ProgDesc& P, const DevOp& op, char* smem, char* scratch) {
+  char* big = smem;
+  SmallSmem<T>* sm = reinterpret_cast<SmallSmem<T>*>(smem + Layout<T>::big);
+  switch (op.kind) {
+    case OP_GATE1:
+      op_gate1<T>(P, op, sm);
+      break;
+    case OP_GATE2:
+      op_gate2<T>(P, op, big, sm, scratch);
+      break;
+    case OP_MOVE_R:
+      op_move_r<T>(P, op, big, sm, scratch);
+      break;
+    case OP_MOVE_L:
+      op_move_l<T>(P, op, big, sm, scratch);
+      break;
+    default:
+      break;
+  }
+}
+__device__ __noinline__ void run_one_op_f64(const ProgDesc& P, const DevOp& op, char* smem, char* scratch) {
+  run_one_op<double>(P, op, smem, scratch);
 }
 
 // Dynamic shared memory and global scratch per CTA of the persistent kernel:
@@ -1426,10 +1466,95 @@ k_run_ops(const ProgDesc* __restrict__ progs, int n_progs, int* queue, char* scr
   }
 }
 
+// Site-parallel run of ONE program: its two-site updates on disjoint sites
+// run on different SMs at once.  Ops are claimed in program order from an
+// atomic counter; op o waits until every earlier op on its sites has
+// finished: deps[o] = (earlier ops on its first site, on its second site or
+// -1), and done[s] counts the finished ops on site s.  Each op reads its
+// sites and the bonds around them only (bond[lo] and bond[lo+2] belong to
+// the ops on sites lo and lo+1), so every op computes exactly what it
+// computes in program order.  No deadlock: an op only waits for ops claimed
+// before it by CTAs that are already running, and the earliest unfinished
+// op waits for nothing.  A wait is bounded (kDepWaitNs): past it the CTA sets
+// ERR_TIMEOUT in the program's error word and every CTA leaves.
+constexpr long long kDepWaitNs = 2000000000LL;
+
+__device__ __forceinline__ long long dag_timer() {
+  long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ int ld_acquire(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__global__ void __launch_bounds__(kOpThreads, 1)
+k_run_ops_sites(const ProgDesc* __restrict__ progs, const int2* __restrict__ deps, int* ctr, char* scratch_base,
+                size_t scratch_stride) {
+  extern __shared__ __align__(16) char smem[];
+  __shared__ int s_op, s_ok;
+  const ProgDesc P = progs[0];
+  int* next = ctr;      // op counter
+  int* done = ctr + 1;  // finished ops per site
+  char* scratch = scratch_base + scratch_stride * blockIdx.x;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      const int o = atomicAdd(next, 1);
+      int ok = 1;
+      if (o < P.n_ops) {
+        const DevOp& op = P.ops[o];
+        const int2 d = deps[o];
+        const int s0 = op.kind == OP_MOVE_L ? op.site - 1 : op.site;
+        const bool two = op.kind != OP_GATE1;
+        long long t0 = -1;
+        for (unsigned int polls = 1;; ++polls) {
+          if (ld_acquire(done + s0) >= d.x && (!two || ld_acquire(done + s0 + 1) >= d.y)) break;
+          if ((polls & 255u) == 0u) {
+            if (*(volatile int*)P.err & ERR_TIMEOUT) {
+              ok = 0;
+              break;
+            }
+            const long long t = dag_timer();
+            if (t0 < 0) {
+              t0 = t;
+            } else if (t - t0 > kDepWaitNs) {
+              atomicOr(P.err, ERR_TIMEOUT);
+              ok = 0;
+              break;
+            }
+          }
+        }
+      }
+      s_op = o;
+      s_ok = ok;
+    }
+    __syncthreads();
+    const int o = s_op;
+    if (o >= P.n_ops || !s_ok) break;
+    const DevOp& op = P.ops[o];
+    if (P.prec == 0)
+      run_one_op_f64(P, op, smem, scratch);
+    else
+      run_one_op<float>(P, op, smem, scratch);
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      const int s0 = op.kind == OP_MOVE_L ? op.site - 1 : op.site;
+      asm volatile("red.release.gpu.global.add.s32 [%0], 1;" ::"l"(done + s0) : "memory");
+      if (op.kind != OP_GATE1) asm volatile("red.release.gpu.global.add.s32 [%0], 1;" ::"l"(done + s0 + 1) : "memory");
+    }
+  }
+  if (threadIdx.x == 0 && blockIdx.x == 0) stat_add(P.stats + ST_N_OPS, (double)P.n_ops);
+}
+
 // ------------------------------------------------------------- launchers
 // Opt in to the large dynamic shared memory once per device (outside any capture).
 cudaError_t configure_ops() {
-  return cudaFuncSetAttribute(k_run_ops, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kOpsSmem);
+  cudaError_t e = cudaFuncSetAttribute(k_run_ops, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kOpsSmem);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_run_ops_sites, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kOpsSmem);
 }
 
 size_t op_scratch_bytes() { return kOpsScratch; }
@@ -1438,6 +1563,12 @@ size_t op_smem_bytes() { return kOpsSmem; }
 cudaError_t launch_ops(const ProgDesc* d_progs, int n_progs, int grid, int* d_queue, char* scratch,
                        cudaStream_t st) {
   k_run_ops<<<grid, kOpThreads, kOpsSmem, st>>>(d_progs, n_progs, d_queue, scratch, kOpsScratch);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ops_sites(const ProgDesc* d_prog, const int2* d_deps, int* d_ctr, int grid, char* scratch,
+                             cudaStream_t st) {
+  k_run_ops_sites<<<grid, kOpThreads, kOpsSmem, st>>>(d_prog, d_deps, d_ctr, scratch, kOpsScratch);
   return cudaGetLastError();
 }
 

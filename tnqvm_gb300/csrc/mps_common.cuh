@@ -106,6 +106,7 @@ enum StatSlot {
 enum ErrBits : int32_t {
   ERR_NAN = 1,        // non-finite value met in a split
   ERR_DIMS = 2,       // bond dimension beyond what the kernel supports
+  ERR_TIMEOUT = 4,    // a site-parallel op waited past its bound for an earlier op
 };
 
 struct ProgDesc {

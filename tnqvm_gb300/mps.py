@@ -17,7 +17,7 @@ OK, ERR_ARG, ERR_OOM, ERR_TIMEOUT, ERR_NUMERIC, ERR_CUDA, ERR_STATE, ERR_UNSUPPO
 TRUNC_EXATN, TRUNC_ITENSOR = 0, 1
 PREC_FP64, PREC_FP32, PREC_AUTO, PREC_SPLIT_BF16 = 0, 1, 2, 3
 AUTO_FP64_QUBITS = 12
-FLAG_RENORM, FLAG_PER_GATE, FLAG_SWEEP, FLAG_FUSE, FLAG_DENSITY = 1, 2, 4, 8, 16
+FLAG_RENORM, FLAG_PER_GATE, FLAG_SWEEP, FLAG_FUSE, FLAG_DENSITY, FLAG_PARALLEL = 1, 2, 4, 8, 16, 32
 DM_QUBITS_MAX, DIAG_QUBITS_MAX = 13, 24
 CHI_LIMIT = 64
 WIDE_CHI_LIMIT = 1024

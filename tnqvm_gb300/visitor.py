@@ -14,7 +14,9 @@ Options (``setOptions``), as in ``TNQVM::updateConfiguration``
 (``ExaTnMpsVisitor.cpp:257-271``): ``svd-cutoff`` (default DBL_MIN),
 ``max-bond-dim`` (default: the build's limit), ``shots``, ``seed``, plus
 ``truncation-mode`` (``exatn`` | ``itensor``), ``precision`` (``fp64`` |
-``fp32``), ``renormalize``, ``per-gate`` (one launch per gate), and for bond
+``fp32``), ``renormalize``, ``per-gate`` (one launch per gate), ``parallel``
+(default on: a circuit's two-site updates on disjoint sites run on different
+SMs at once; results unchanged), and for bond
 caps above 64 ``gemm-autotune`` (0 static, 1 tune, 2 table) and
 ``gemm-tune-cache`` (a saved tuning table, used without trial launches).
 """
@@ -121,6 +123,9 @@ class GpuMpsVisitor:
                 "split-bf16": M.PREC_SPLIT_BF16}[o.get("precision", "fp64")]
         flags = (M.FLAG_RENORM if o.get("renormalize", False) else 0) | \
                 (M.FLAG_PER_GATE if o.get("per-gate", False) else 0)
+        # independent two-site updates on different SMs (default on; same results)
+        if o.get("parallel", True) and not (flags & M.FLAG_PER_GATE):
+            flags |= M.FLAG_PARALLEL
         cutoff = float(o["svd-cutoff"]) if "svd-cutoff" in o else -1.0
         chi = int(o["max-bond-dim"]) if "max-bond-dim" in o else 0
         # GEMM kernel choice of the wide path (no counterpart in the reference)

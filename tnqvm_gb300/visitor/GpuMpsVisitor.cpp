@@ -72,6 +72,9 @@ void GpuMpsVisitor::initialize(std::shared_ptr<AcceleratorBuffer> in_buffer, int
   int flags = 0;
   if (options.keyExists<bool>("renormalize") && options.get<bool>("renormalize")) flags |= MPS_FLAG_RENORM;
   if (options.keyExists<bool>("per-gate") && options.get<bool>("per-gate")) flags |= MPS_FLAG_PER_GATE;
+  // independent two-site updates on different SMs (default on; same results)
+  const bool parallel = !(options.keyExists<bool>("parallel") && !options.get<bool>("parallel"));
+  if (parallel && !(flags & MPS_FLAG_PER_GATE)) flags |= MPS_FLAG_PARALLEL;
   // GEMM kernel choice of the wide path (bond caps above 64); no counterpart in
   // the reference: "gemm-tune-cache" loads a saved table and uses it without
   // trial launches, "gemm-autotune" sets the mode (0 static, 1 tune, 2 table)
