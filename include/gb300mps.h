@@ -352,6 +352,12 @@ int mps_diag_cgemm_kind(mps_ctx* ctx, int precision, int kernel, int flags, int 
  * independent FMA chains on every SM timed with CUDA events: the roofline
  * denominator of the kernels that run on CUDA cores. */
 int mps_diag_fma_rate(int device, int precision, double* flops_per_s);
+/* Diagnostic: most CTAs a site-parallel run (MPS_FLAG_PARALLEL) may use,
+ * process-wide (0 = as many as the program's sites allow, the default).
+ * With 1 the run executes its ops one after another on the same kernel,
+ * the bit-for-bit reference of a wider run.  No counterpart in the
+ * reference. */
+int mps_diag_set_parallel_width(int max_ctas);
 
 /* Footprint used by admission: sum over sites of chi_l * 2 * chi_r * bytes. */
 size_t mps_footprint_bytes(int n_qubits, int chi_max, int precision);

@@ -84,3 +84,52 @@ def test_plugin_vqe_basis_signs():
         out = _run(n, 0, circ, [("truncation-mode", "itensor")], obs)
         want = sign * dense.expect_pauli(psi, n, "XIY").real
         assert abs(out["vqe-exp-val"] - want) < 1e-10, (t, out["vqe-exp-val"], want)
+
+
+def _noise_lines(model_json):
+    """The demo driver's noise-model lines for a JSON noise model."""
+    doc = json.loads(model_json)
+    lines = []
+    for e in doc.get("gate_noise", []):
+        qs = [int(x) for x in e["register_location"]]
+        for ch in e["noise_channels"]:
+            flat = []
+            for k in ch["matrix"]:
+                for row in k:
+                    for v in row:
+                        flat += [v[0], v[1]]
+            lines.append(("noise", "%s %d %s %d %s" % (e["gate_name"], len(qs), " ".join(map(str, qs)),
+                                                      len(ch["matrix"]), " ".join("%.17g" % x for x in flat))))
+    for e in doc.get("readout_errors", []):
+        lines.append(("readout", "%s %.17g %.17g" % (e["register_location"], e["prob_meas0_prep1"],
+                                                     e["prob_meas1_prep0"])))
+    return lines
+
+
+def _run_pmps(n, shots, circ, model_json=None, opts=()):
+    exe = B.build_visitor_demo()
+    script = _script(n, shots, circ, [("visitor", "pmps")] + list(opts))
+    head, rest = script.split("\n", 1)
+    extra = "".join("%s %s\n" % kv for kv in (_noise_lines(model_json) if model_json else []))
+    r = subprocess.run([exe], input=head + "\n" + extra + rest, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    return json.loads(r.stdout)
+
+
+@pytest.mark.gpu
+def test_plugin_pmps_noise_model_goldens():
+    """The noisy visitor through the C++ plugin against the reference's
+    JsonNoiseModelTester.cpp: depolarizing after X gives density_matrix
+    diag(0.00666667, 0.99333333); readout errors P(1|0) = 0.1 +- 0.05."""
+    import os
+    gold = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "noise_models.json")))
+    g = gold["depolarizing"]
+    out = _run_pmps(1, 1024, [("X", (0,), ()), ("Measure", (0,), ())], g["model"], [("seed", 1)])
+    assert out["name"] == "gb300-pmps"
+    dm = out["density_matrix"]
+    for (re, im), want in zip(dm, g["density_matrix_real"]):
+        assert abs(re - want) < g["tolerance"] and abs(im) < 1e-6
+    r = gold["readout"]
+    out = _run_pmps(1, 8192, [("Measure", (0,), ())], r["model"], [("seed", 2)])
+    p1 = out["counts"].get("1", 0) / 8192
+    assert abs(p1 - r["prob_1_prep_0"]) < r["tolerance"]

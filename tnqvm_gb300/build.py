@@ -72,7 +72,7 @@ def build_visitor_demo():
     """Compile the C++ TNQVM visitor plugin (shim build) and its driver, linked
     against libgb300mps.so."""
     lib = build()
-    srcs = [os.path.join(VISITOR_DIR, f) for f in ("GpuMpsVisitor.cpp", "visitor_demo.cpp")]
+    srcs = [os.path.join(VISITOR_DIR, f) for f in ("GpuMpsVisitor.cpp", "GpuPmpsVisitor.cpp", "visitor_demo.cpp")]
     deps = srcs + [os.path.join(VISITOR_DIR, f) for f in os.listdir(VISITOR_DIR) if f.endswith(".hpp")] + [lib]
     if not _stale(VISITOR_DEMO, deps):
         return VISITOR_DEMO

@@ -20,6 +20,7 @@
 namespace gbmps {
 
 thread_local std::string g_err;
+static std::atomic<int> g_parallel_width{0};  // mps_diag_set_parallel_width
 
 int fail(int code, const std::string& msg) {
   g_err = msg;
@@ -444,7 +445,9 @@ int launch_programs(mps_ctx* c, Lane& L, mps_prog* const* progs_in, int n_in, bo
         host[2 * o] = seen[s0]++;
         host[2 * o + 1] = op.kind == OP_GATE1 ? -1 : seen[s0 + 1]++;
       }
-      const int width = std::max(1, p->n / 2);  // two-site ops that can run at once
+      int width = std::max(1, p->n / 2);  // two-site ops that can run at once
+      const int cap = g_parallel_width.load();
+      if (cap > 0) width = std::min(width, cap);
       rc = grow(&L.d_dag, &L.d_dag_cap, host.size());
       if (rc) return rc;
       e = cudaMemcpyAsync(L.d_dag, host.data(), host.size() * sizeof(int), cudaMemcpyHostToDevice, L.stream);
@@ -1301,6 +1304,12 @@ int mps_autotune_tunings(mps_ctx* c, int* out) {
   if (!c || !out) return fail(MPS_ERR_ARG, "NULL argument");
   std::lock_guard<std::mutex> lk(c->mu);
   *out = wide_gemm_tunings(c);
+  return MPS_OK;
+}
+
+int mps_diag_set_parallel_width(int max_ctas) {
+  if (max_ctas < 0) return fail(MPS_ERR_ARG, "max_ctas must be >= 0");
+  g_parallel_width.store(max_ctas);
   return MPS_OK;
 }
 

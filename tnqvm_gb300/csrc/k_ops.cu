@@ -1343,29 +1343,51 @@ __device__ void op_move_l(const ProgDesc& P, const DevOp& op, char* big, SmallSm
 
 // One program on this CTA, in its own precision: its ops in order, then its
 // attached observables, then the completion flag of the serve loop.
+// One op of a program on this CTA.  Each precision's op body is one
+// non-inlined function that both the persistent kernel (program order) and
+// the site-parallel kernel call, so the two runs execute the same machine
+// code for every op and give bit-identical results.
+template <typename T>
+__device__ __forceinline__ void run_one_op(const ProgDesc& P, const DevOp& op, char* smem, char* scratch) {
+  char* big = smem;
+  SmallSmem<T>* sm = reinterpret_cast<SmallSmem<T>*>(smem + Layout<T>::big);
+  switch (op.kind) {
+    case OP_GATE1:
+      op_gate1<T>(P, op, sm);
+      break;
+    case OP_GATE2:
+      op_gate2<T>(P, op, big, sm, scratch);
+      break;
+    case OP_MOVE_R:
+      op_move_r<T>(P, op, big, sm, scratch);
+      break;
+    case OP_MOVE_L:
+      op_move_l<T>(P, op, big, sm, scratch);
+      break;
+    default:
+      break;
+  }
+}
+__device__ __noinline__ void run_one_op_f64(const ProgDesc& P, const DevOp& op, char* smem, char* scratch) {
+  run_one_op<double>(P, op, smem, scratch);
+}
+__device__ __noinline__ void run_one_op_f32(const ProgDesc& P, const DevOp& op, char* smem, char* scratch) {
+  run_one_op<float>(P, op, smem, scratch);
+}
+template <typename T>
+__device__ __forceinline__ void run_op(const ProgDesc& P, const DevOp& op, char* smem, char* scratch) {
+  if (sizeof(T) == 8)
+    run_one_op_f64(P, op, smem, scratch);
+  else
+    run_one_op_f32(P, op, smem, scratch);
+}
+
 template <typename T>
 __device__ void run_program(const ProgDesc& P, char* smem, char* scratch) {
   const long long c_begin = clock64();
   char* big = smem;
-  SmallSmem<T>* sm = reinterpret_cast<SmallSmem<T>*>(smem + Layout<T>::big);
   for (int o = 0; o < P.n_ops; ++o) {
-    const DevOp& op = P.ops[o];
-    switch (op.kind) {
-      case OP_GATE1:
-        op_gate1<T>(P, op, sm);
-        break;
-      case OP_GATE2:
-        op_gate2<T>(P, op, big, sm, scratch);
-        break;
-      case OP_MOVE_R:
-        op_move_r<T>(P, op, big, sm, scratch);
-        break;
-      case OP_MOVE_L:
-        op_move_l<T>(P, op, big, sm, scratch);
-        break;
-      default:
-        break;
-    }
+    run_op<T>(P, P.ops[o], smem, scratch);
     __syncthreads();
   }
   if (threadIdx.x == 0) stat_add(P.stats + ST_N_OPS, (double)P.n_ops);
@@ -1408,31 +1430,6 @@ __device__ __noinline__ void run_program_f64(const ProgDesc& P, char* smem, char
   run_program<double>(P, smem, scratch);
 }
 
-// One op of a program on this CTA.
-template <typename T>
-__device__ void run_one_op(const ProgDesc& P, const DevOp& op, char* smem, char* scratch) {
-  char* big = smem;
-  SmallSmem<T>* sm = reinterpret_cast<SmallSmem<T>*>(smem + Layout<T>::big);
-  switch (op.kind) {
-    case OP_GATE1:
-      op_gate1<T>(P, op, sm);
-      break;
-    case OP_GATE2:
-      op_gate2<T>(P, op, big, sm, scratch);
-      break;
-    case OP_MOVE_R:
-      op_move_r<T>(P, op, big, sm, scratch);
-      break;
-    case OP_MOVE_L:
-      op_move_l<T>(P, op, big, sm, scratch);
-      break;
-    default:
-      break;
-  }
-}
-__device__ __noinline__ void run_one_op_f64(const ProgDesc& P, const DevOp& op, char* smem, char* scratch) {
-  run_one_op<double>(P, op, smem, scratch);
-}
 
 // Dynamic shared memory and global scratch per CTA of the persistent kernel:
 // enough for a program of either precision.
@@ -1537,7 +1534,7 @@ k_run_ops_sites(const ProgDesc* __restrict__ progs, const int2* __restrict__ dep
     if (P.prec == 0)
       run_one_op_f64(P, op, smem, scratch);
     else
-      run_one_op<float>(P, op, smem, scratch);
+      run_one_op_f32(P, op, smem, scratch);
     __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) {

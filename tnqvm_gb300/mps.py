@@ -94,6 +94,7 @@ SIGNATURES = [
     ("mps_autotune_clear", _c.c_int, []),
     ("mps_autotune_tunings", _c.c_int, [_P, _c.POINTER(_c.c_int)]),
     ("mps_channel1", _c.c_int, [_P, _c.c_int, _c.c_int, _DP]),
+    ("mps_diag_set_parallel_width", _c.c_int, [_c.c_int]),
     ("mps_density_matrix", _c.c_int, [_P, _c.c_int, _c.POINTER(_c.c_int), _DP]),
     ("mps_density_diag", _c.c_int, [_P, _c.c_int, _c.POINTER(_c.c_int), _DP]),
 ]
@@ -270,6 +271,13 @@ def fma_rate(device=0, precision=PREC_FP32):
     v = ctypes.c_double()
     _check(_lib.mps_diag_fma_rate(device, precision, ctypes.byref(v)))
     return v.value
+
+
+def set_parallel_width(max_ctas):
+    """Most CTAs a site-parallel run may use (0 = automatic); 1 runs the same
+    kernel one op at a time."""
+    load_library()
+    _check(_lib.mps_diag_set_parallel_width(max_ctas))
 
 
 def autotune_set_mode(mode):
@@ -512,6 +520,11 @@ class Program:
         _check(_lib.mps_bond_dims(self.h, out))
         return list(out)[: self.n - 1]
 
+    def stats(self):
+        out = np.zeros(4)
+        _check(_lib.mps_stats(self.h, _dptr(out)))
+        return {"fidelity": out[0], "max_discarded": out[1], "gate2": int(out[2]), "ops": int(out[3])}
+
     # ---- noisy circuits (DensityProgram)
     def channel(self, q, kraus):
         """rho -> sum_k K_k rho K_k^H on qubit q (density programs)."""
@@ -550,8 +563,3 @@ class DensityProgram(Program):
         out = (ctypes.c_int * (m - 1))()
         _check(_lib.mps_bond_dims(self.h, out))
         return list(out)
-
-    def stats(self):
-        out = np.zeros(4)
-        _check(_lib.mps_stats(self.h, _dptr(out)))
-        return {"fidelity": out[0], "max_discarded": out[1], "gate2": int(out[2]), "ops": int(out[3])}

@@ -153,4 +153,20 @@ GB300_SHIM_GATES(GB300_GATE)
 std::shared_ptr<Instruction> make_gate(const std::string& name, std::vector<std::size_t> bits,
                                        std::vector<double> params = {});
 }  // namespace quantum
+
+// The two NoiseModel calls the noisy visitor makes (ExaTnPmpsVisitor.cpp
+// :157-160,838-847): the Kraus channels that follow a gate, and a qubit's
+// readout error as (P(meas 0 | prep 1), P(meas 1 | prep 0)).
+enum class KrausMatBitOrder { MSB, LSB };
+struct NoiseChannelKraus {
+  std::vector<std::size_t> noise_qubits;
+  std::vector<std::vector<std::vector<std::complex<double>>>> mats;
+  KrausMatBitOrder bit_order = KrausMatBitOrder::MSB;
+};
+class NoiseModel {
+ public:
+  virtual ~NoiseModel() = default;
+  virtual std::vector<NoiseChannelKraus> getNoiseChannels(Instruction& gate) = 0;
+  virtual std::pair<double, double> readoutError(std::size_t qubit) = 0;
+};
 }  // namespace xacc
