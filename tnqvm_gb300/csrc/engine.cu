@@ -434,17 +434,41 @@ int launch_programs(mps_ctx* c, Lane& L, mps_prog* const* progs_in, int n_in, bo
       }
     } else if (n == 1 && nd == 1 && (progs[0]->flags & MPS_FLAG_PARALLEL) && progs[0]->serve_flag == nullptr &&
                flat.size() > 1) {
-      // site-parallel: per op, the number of earlier ops on each of its sites
+      // site-parallel.  Ops are handed out by level (1 + the level of the
+      // previous op on each of their sites), program order within a level:
+      // ops of one level are independent, so the CTAs claiming them run at
+      // once instead of queueing behind a chain, and every site still sees
+      // its ops in program order (a later op on a site has a higher level).
+      // Per op: the number of earlier ops on each of its sites.
       const mps_prog* p = progs[0];
       const size_t nops = flat.size();
-      std::vector<int> host((nops * 2) + 1 + p->n, 0);
-      std::vector<int> seen(p->n, 0);
+      std::vector<int> level(nops), last(p->n, 0);
       for (size_t o = 0; o < nops; ++o) {
         const DevOp& op = flat[o];
         const int s0 = op.kind == OP_MOVE_L ? op.site - 1 : op.site;
-        host[2 * o] = seen[s0]++;
-        host[2 * o + 1] = op.kind == OP_GATE1 ? -1 : seen[s0 + 1]++;
+        const bool two = op.kind != OP_GATE1;
+        const int l = 1 + std::max(last[s0], two ? last[s0 + 1] : 0);
+        level[o] = l;
+        last[s0] = l;
+        if (two) last[s0 + 1] = l;
       }
+      std::vector<int> order(nops);
+      for (size_t o = 0; o < nops; ++o) order[o] = (int)o;
+      std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return level[a] < level[b]; });
+      std::vector<DevOp> sorted(nops);
+      std::vector<int> host((nops * 2) + 1 + p->n, 0);
+      std::vector<int> seen(p->n, 0);
+      for (size_t k = 0; k < nops; ++k) {
+        const DevOp& op = flat[order[k]];
+        sorted[k] = op;
+        const int s0 = op.kind == OP_MOVE_L ? op.site - 1 : op.site;
+        host[2 * k] = seen[s0]++;
+        host[2 * k + 1] = op.kind == OP_GATE1 ? -1 : seen[s0 + 1]++;
+      }
+      // pageable source: staged before the call returns; lands over the
+      // program-order table uploaded above
+      e = cudaMemcpyAsync(L.d_ops, sorted.data(), nops * sizeof(DevOp), cudaMemcpyHostToDevice, L.stream);
+      if (e != cudaSuccess) return fail(MPS_ERR_CUDA, cudaGetErrorString(e));
       int width = std::max(1, p->n / 2);  // two-site ops that can run at once
       const int cap = g_parallel_width.load();
       if (cap > 0) width = std::min(width, cap);

@@ -209,30 +209,56 @@ int mps_graph_create(mps_ctx* c, mps_prog* const* progs, int n, mps_graph** out)
   return MPS_OK;
 }
 
+// Programs compile independently, so an update compiles them on host
+// threads, checks that each keeps its op structure (kind, site, orientation
+// of every op: the captured launch depends on it) and writes its ops straight
+// into the pinned staging buffer, from which one copy goes to the device.
 int mps_graph_update(mps_graph* g) {
   if (!g) return fail(MPS_ERR_ARG, "NULL graph");
   GCK(cudaSetDevice(g->c->device));
-  std::vector<DevOp> flat;
-  std::vector<size_t> first, count;
-  build_ops(g, flat, first, count);
-  if (count != g->count) return fail(MPS_ERR_ARG, "update changes the circuit structure");
-  for (size_t i = 0; i < flat.size(); ++i)
-    if (flat[i].kind != g->flat[i].kind || flat[i].site != g->flat[i].site || flat[i].orient != g->flat[i].orient)
-      return fail(MPS_ERR_ARG, "update changes the circuit structure");
-  g->flat.swap(flat);
-  if (g->flat.empty()) return MPS_OK;
-  const size_t bytes = g->flat.size() * sizeof(DevOp);
-  if (!g->h_ops) {
-    if (cudaMallocHost(&g->h_ops, bytes) != cudaSuccess || cudaEventCreateWithFlags(&g->copied_ev,
-                                                                                    cudaEventDisableTiming) !=
-                                                                 cudaSuccess) {
-      cudaGetLastError();
-      return fail(MPS_ERR_OOM, "pinned op-table staging failed");
+  const size_t np = g->progs.size();
+  const size_t total = g->flat.size();
+  const size_t bytes = total * sizeof(DevOp);
+  if (total > 0) {
+    if (!g->h_ops) {
+      if (cudaMallocHost(&g->h_ops, bytes) != cudaSuccess ||
+          cudaEventCreateWithFlags(&g->copied_ev, cudaEventDisableTiming) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(MPS_ERR_OOM, "pinned op-table staging failed");
+      }
+    } else {
+      GCK(cudaEventSynchronize(g->copied_ev));  // the previous copy has left the staging buffer
     }
-  } else {
-    GCK(cudaEventSynchronize(g->copied_ev));  // the previous copy has left the staging buffer
   }
-  std::memcpy(g->h_ops, g->flat.data(), bytes);
+  std::atomic<size_t> next{0};
+  std::atomic<int> changed{0};
+  auto work = [&]() {
+    std::vector<DevOp> ops;
+    for (size_t i; (i = next.fetch_add(1)) < np;) {
+      mps_prog* p = g->progs[i];
+      p->center = 0;  // every replay starts from |0...0>
+      compile_program(p, ops);
+      if (ops.size() != g->count[i]) {
+        changed.store(1);
+        continue;
+      }
+      const DevOp* old = g->flat.data() + g->first[i];
+      for (size_t k = 0; k < ops.size(); ++k)
+        if (ops[k].kind != old[k].kind || ops[k].site != old[k].site || ops[k].orient != old[k].orient) {
+          changed.store(1);
+          break;
+        }
+      if (!ops.empty()) std::memcpy(g->h_ops + g->first[i], ops.data(), ops.size() * sizeof(DevOp));
+    }
+  };
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  const int nt = (int)std::min<size_t>({(size_t)hw, (size_t)16, std::max<size_t>(np / 32, 1)});
+  std::vector<std::thread> pool;
+  for (int t = 1; t < nt; ++t) pool.emplace_back(work);
+  work();
+  for (auto& t : pool) t.join();
+  if (changed.load()) return fail(MPS_ERR_ARG, "update changes the circuit structure");
+  if (total == 0) return MPS_OK;
   GCK(cudaMemcpyAsync(g->L.d_ops, g->h_ops, bytes, cudaMemcpyHostToDevice, g->L.stream));
   GCK(cudaEventRecord(g->copied_ev, g->L.stream));
   return MPS_OK;
