@@ -149,6 +149,13 @@ enum {
   MPS_G_CH, MPS_G_CRZ, MPS_G_ISWAP, MPS_G_FSIM, MPS_G_RZZ, MPS_G_COUNT
 };
 int mps_gates(mps_prog* p, int n_gates, const int32_t* ids, const int32_t* qubits, const double* params);
+/* The same for many programs in one call (e.g. new parameters for every
+ * circuit of a batch): program i records gates first_gate[i] ..
+ * first_gate[i+1]-1 of the concatenated arrays (first_gate has n_progs+1
+ * entries); programs are recorded on host threads.  On failure the first
+ * failing program is reported and the others have recorded their gates. */
+int mps_gates_many(int n_progs, mps_prog* const* progs, const int64_t* first_gate, const int32_t* ids,
+                   const int32_t* qubits, const double* params);
 
 /* Execution.  mps_submit compiles the gates recorded since the previous
  * submit (routing, 1-qubit fusion, gauge moves) and enqueues them; the MPS

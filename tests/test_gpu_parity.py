@@ -519,3 +519,23 @@ def test_admission_budget():
         b.close()
         d.close()
         assert c2.bytes_resident == 0
+
+
+def test_batch_record_equals_per_program_record(ctx):
+    """mps_gates_many (every program's gates in one call, recorded on host
+    threads) gives the same programs as one mps_gates call per program."""
+    insts = circuits.vqe_batch(12, seed=9, qmax=14)
+    encs = [M.encode_circuit(it["circuit"]) for it in insts]
+    a = [M.Program(ctx, it["n"], 64, 1e-12, M.TRUNC_ITENSOR, M.PREC_FP64) for it in insts]
+    b = [M.Program(ctx, it["n"], 64, 1e-12, M.TRUNC_ITENSOR, M.PREC_FP64) for it in insts]
+    try:
+        for p, e in zip(a, encs):
+            p.record(e)
+        M.BatchRecord(b, encs).record()
+        for p, q, it in zip(a, b, insts):
+            p.set_observable(it["paulis"], it["coeffs"])
+            q.set_observable(it["paulis"], it["coeffs"])
+        assert np.array_equal(ctx.batch_expect(a), ctx.batch_expect(b))
+    finally:
+        for p in a + b:
+            p.close()

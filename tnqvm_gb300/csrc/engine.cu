@@ -3,7 +3,10 @@
 // result read-back.  All device work goes through the kernels in k_ops.cu and
 // k_measure.cu; there is no CPU execution path.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
+#include <climits>
+#include <cstdint>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -941,6 +944,38 @@ int mps_gates(mps_prog* p, int n_gates, const int32_t* ids, const int32_t* qubit
     const int rc = mps_gate_named(p, kNames[id], qubits + 2 * g, kNq[id], params + 3 * g, kNp[id]);
     if (rc) return rc;
   }
+  return MPS_OK;
+}
+
+int mps_gates_many(int n_progs, mps_prog* const* progs, const int64_t* first_gate, const int32_t* ids,
+                   const int32_t* qubits, const double* params) {
+  if (n_progs < 0 || (n_progs > 0 && (!progs || !first_gate || !ids || !qubits || !params)))
+    return fail(MPS_ERR_ARG, "NULL argument");
+  for (int i = 0; i < n_progs; ++i) {
+    if (!progs[i]) return fail(MPS_ERR_ARG, "NULL program");
+    if (first_gate[i + 1] < first_gate[i] || first_gate[i + 1] - first_gate[i] > INT32_MAX)
+      return fail(MPS_ERR_ARG, "first_gate must be non-decreasing");
+  }
+  // programs record independently: host threads, the first failure (lowest
+  // program index) is reported
+  std::vector<int> rcs(n_progs, MPS_OK);
+  std::vector<std::string> msgs(n_progs);
+  std::atomic<int> next{0};
+  auto work = [&]() {
+    for (int i; (i = next.fetch_add(1)) < n_progs;) {
+      const int64_t f = first_gate[i];
+      rcs[i] = mps_gates(progs[i], (int)(first_gate[i + 1] - f), ids + f, qubits + 2 * f, params + 3 * f);
+      if (rcs[i]) msgs[i] = g_err;
+    }
+  };
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  const int nt = (int)std::min<long long>({(long long)hw, 16LL, std::max<long long>(n_progs / 32, 1)});
+  std::vector<std::thread> pool;
+  for (int t = 1; t < nt; ++t) pool.emplace_back(work);
+  work();
+  for (auto& t : pool) t.join();
+  for (int i = 0; i < n_progs; ++i)
+    if (rcs[i]) return fail(rcs[i], "program " + std::to_string(i) + ": " + msgs[i]);
   return MPS_OK;
 }
 

@@ -79,6 +79,8 @@ SIGNATURES = [
     ("mps_graph_phase_cycles", _c.c_int, [_P, _DP]),
     ("mps_graph_stat_sums", _c.c_int, [_P, _DP, _c.c_int]),
     ("mps_gates", _c.c_int, [_P, _c.c_int, _c.POINTER(_c.c_int32), _c.POINTER(_c.c_int32), _DP]),
+    ("mps_gates_many", _c.c_int, [_c.c_int, _c.POINTER(_P), _c.POINTER(_c.c_int64), _c.POINTER(_c.c_int32),
+                                  _c.POINTER(_c.c_int32), _DP]),
     ("mps_gate2_apply_noalloc", _c.c_int, [_c.c_int, _c.c_int, _c.c_int, _c.c_double, _P, _c.c_int64,
                                             _P, _c.POINTER(_c.c_int), _DP, _P]),
     ("mps_diag_cgemm", _c.c_int, [_P, _c.c_int, _c.c_int, _c.c_int, _DP, _DP, _DP, _DP]),
@@ -382,6 +384,28 @@ class Graph:
         if self.h:
             _lib.mps_graph_destroy(self.h)
             self.h = None
+
+
+class BatchRecord:
+    """Many programs' ``encode_circuit`` results concatenated once, then
+    recorded on all of them by one C call (``mps_gates_many``; the library
+    records the programs on host threads)."""
+
+    def __init__(self, programs, encoded):
+        self.programs = list(programs)
+        self.arr = (ctypes.c_void_p * len(self.programs))(*[p.h for p in self.programs])
+        counts = [len(e[0]) for e in encoded]
+        self.first = np.zeros(len(counts) + 1, dtype=np.int64)
+        self.first[1:] = np.cumsum(counts)
+        self.ids = np.ascontiguousarray(np.concatenate([e[0] for e in encoded]), dtype=np.int32)
+        self.qs = np.ascontiguousarray(np.concatenate([e[1] for e in encoded]), dtype=np.int32)
+        self.ps = np.ascontiguousarray(np.concatenate([e[2] for e in encoded]), dtype=np.float64)
+
+    def record(self):
+        _check(_lib.mps_gates_many(len(self.programs), self.arr,
+                                   self.first.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+                                   self.ids.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                                   self.qs.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), _dptr(self.ps)))
 
 
 def footprint_bytes(n, chi_max, precision):
