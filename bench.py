@@ -440,8 +440,8 @@ def noisy_circuits(ctx):
     visitor): an 8-qubit brick wall of depth 8 (U3 + CNOT) with a
     depolarizing channel (p = 0.01) on both qubits after every CNOT, complex128,
     exact (bond cap 256 on the 16-site doubled chain: the wide path) and
-    truncated (cap 32), each against the dense density-matrix oracle: <Z_i>
-    for every qubit and the trace."""
+    truncated (cap 128), each against the dense density-matrix oracle: <Z_i>
+    (normalised by the trace) for every qubit, and the trace."""
     from tnqvm_gb300 import circuits
     from tnqvm_gb300 import mps as M
     from oracle import density as R
@@ -462,9 +462,9 @@ def noisy_circuits(ctx):
     out = {"workload": "8-qubit brick wall, depth 8, U3 + CNOT, depolarizing p=0.01 on both qubits after "
                        "every CNOT; complex128 density program (16-site doubled chain)",
            "dense_oracle_cpu_seconds": cpu_s}
-    for chi in (256, 32):
+    for chi in (256, 128):
         t0 = time.perf_counter()
-        p = M.DensityProgram(ctx, n, chi, 1e-14, M.TRUNC_ITENSOR, M.PREC_FP64)
+        p = M.DensityProgram(ctx, n, chi, 1e-300, M.TRUNC_ITENSOR, M.PREC_FP64)
         for name, qs, ps in circ:
             if name == "Kraus":
                 p.channel(qs[0], ps)

@@ -172,53 +172,64 @@ __device__ void householder_qr(cx<T>* M, int mr, int nc, int ld, cx<T>* Rb, Smal
   const int tid = threadIdx.x, nt = blockDim.x;
   const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
   const int k = mr < nc ? mr : nc;
-  for (int j = 0; j < k; ++j) {
-    // warp 0: norm, reflector scalars (working precision) and the scaled column
-    if (warp == 0) {
-      T s = T(0);
-      for (int i = j + 1 + lane; i < mr; i += 32) s += abs2(M[i * ld + j]);
-      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-      const cx<T> alpha = M[j * ld + j];
-      __syncwarp();  // every lane has read alpha before lane 0 overwrites it with beta
-      const T ar = alpha.re, ai = alpha.im;
-      const T nrm2 = ar * ar + ai * ai + s;
-      // a column below ~sqrt(tiny) is left as is (its reflector scale would overflow)
-      const bool refl = !(s == T(0) && ai == T(0)) && nrm2 > T(Prec<T>::tiny);
-      T ir = T(0), ii = T(0);
-      if (refl) {
-        const T beta = -copysign(sqrt(nrm2), ar);
-        const T dr = ar - beta, di = ai, den = dr * dr + di * di;
-        ir = dr / den;
-        ii = -di / den;
-        if (lane == 0) {
-          sm->tau[j] = mk<T>((beta - ar) / beta, -ai / beta);
-          M[j * ld + j] = mk<T>(beta, T(0));
-        }
-        for (int i = j + 1 + lane; i < mr; i += 32) {
-          const cx<T> x = M[i * ld + j];
-          M[i * ld + j] = mk<T>(x.re * ir - x.im * ii, x.re * ii + x.im * ir);
-        }
-      } else if (lane == 0) {
-        sm->tau[j] = mk<T>(0, 0);
+  // warp 0: reflector of column jj (norm, scalars in working precision, the
+  // scaled column); tau[jj] = 0 when the column is left as is
+  auto reflector = [&](int jj) {
+    T s = T(0);
+    for (int i = jj + 1 + lane; i < mr; i += 32) s += abs2(M[i * ld + jj]);
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    const cx<T> alpha = M[jj * ld + jj];
+    __syncwarp();  // every lane has read alpha before lane 0 overwrites it with beta
+    const T ar = alpha.re, ai = alpha.im;
+    const T nrm2 = ar * ar + ai * ai + s;
+    // a column below ~sqrt(tiny) is left as is (its reflector scale would overflow)
+    const bool refl = !(s == T(0) && ai == T(0)) && nrm2 > T(Prec<T>::tiny);
+    if (refl) {
+      const T beta = -copysign(sqrt(nrm2), ar);
+      const T dr = ar - beta, di = ai, den = dr * dr + di * di;
+      const T ir = dr / den, ii = -di / den;
+      if (lane == 0) {
+        // real part 1 - ar / beta >= 1: a reflector always has tau != 0
+        sm->tau[jj] = mk<T>((beta - ar) / beta, -ai / beta);
+        M[jj * ld + jj] = mk<T>(beta, T(0));
       }
-      if (lane == 0) sm->ival[1] = refl ? 1 : 0;
+      for (int i = jj + 1 + lane; i < mr; i += 32) {
+        const cx<T> x = M[i * ld + jj];
+        M[i * ld + jj] = mk<T>(x.re * ir - x.im * ii, x.re * ii + x.im * ir);
+      }
+    } else if (lane == 0) {
+      sm->tau[jj] = mk<T>(0, 0);
     }
-    __syncthreads();
-    if (sm->ival[1]) {
-      const cx<T> ctau = conj(sm->tau[j]);
-      for (int c = j + 1 + warp; c < nc; c += nw) {
-        cx<T> w = mk<T>(0, 0);
-        for (int i = j + 1 + lane; i < mr; i += 32) fma_cj(w, M[i * ld + j], M[i * ld + c]);
-        for (int o = 16; o > 0; o >>= 1) {
-          w.re += __shfl_xor_sync(0xffffffffu, w.re, o);
-          w.im += __shfl_xor_sync(0xffffffffu, w.im, o);
-        }
-        w = w + M[j * ld + c];
-        const cx<T> tw = ctau * w;
-        for (int i = j + 1 + lane; i < mr; i += 32) M[i * ld + c] = M[i * ld + c] - M[i * ld + j] * tw;
-        __syncwarp();
-        if (lane == 0) M[j * ld + c] = M[j * ld + c] - tw;
-      }
+  };
+  // column c <- H_j^H column c (one warp, lanes over rows)
+  auto apply = [&](int j, int c, cx<T> ctau) {
+    cx<T> w = mk<T>(0, 0);
+    for (int i = j + 1 + lane; i < mr; i += 32) fma_cj(w, M[i * ld + j], M[i * ld + c]);
+    for (int o = 16; o > 0; o >>= 1) {
+      w.re += __shfl_xor_sync(0xffffffffu, w.re, o);
+      w.im += __shfl_xor_sync(0xffffffffu, w.im, o);
+    }
+    w = w + M[j * ld + c];
+    const cx<T> tw = ctau * w;
+    for (int i = j + 1 + lane; i < mr; i += 32) M[i * ld + c] = M[i * ld + c] - M[i * ld + j] * tw;
+    __syncwarp();
+    if (lane == 0) M[j * ld + c] = M[j * ld + c] - tw;
+  };
+  // One barrier per column: warp 0 applies reflector j to column j+1 and
+  // forms reflector j+1 from it while warps 1.. apply reflector j to the
+  // columns after it.
+  if (k > 0 && warp == 0) reflector(0);
+  __syncthreads();
+  for (int j = 0; j < k; ++j) {
+    const cx<T> tj = sm->tau[j];
+    const bool has = tj.re != T(0) || tj.im != T(0);
+    const cx<T> ctau = conj(tj);
+    if (warp == 0) {
+      if (has && j + 1 < nc) apply(j, j + 1, ctau);
+      __syncwarp();
+      if (j + 1 < k) reflector(j + 1);
+    } else if (has) {
+      for (int c = j + 2 + (warp - 1); c < nc; c += nw - 1) apply(j, c, ctau);
     }
     __syncthreads();
   }
@@ -280,9 +291,9 @@ __device__ __forceinline__ int eig_ld(int m) {
 // v_j[j+1] = 1 and v_j[i] (i > j+1) stored in A[i][j] (LAPACK zhetd2, lower).
 //
 // Two CTA barriers per column.  Warp 0 forms the reflector of column j+1
-// while the other warps apply step j's rank-2 update: it updates column j+1
-// (the trailing matrix's first column, which no other warp touches) itself,
-// then reduces it.  The reflectors alternate between two buffers, since the
+// while the other warps apply step j's rank-2 update to columns j+2..: it
+// updates column j+1 (the trailing matrix's first column, which no other
+// warp touches) itself, then reduces it.  The reflectors alternate between two buffers, since the
 // other warps still read v_j while warp 0 writes v_{j+1}.
 template <typename T>
 __device__ void tridiagonalize(cx<T>* A, int m, double trace, SmallSmem<T>* sm) {
@@ -387,10 +398,11 @@ __device__ void tridiagonalize(cx<T>* A, int m, double trace, SmallSmem<T>* sm) 
         if (next) reflector(j + 1, b ^ 1);
       }
       if (L >= 32) {
-        // a warp per row, lanes over its columns 1..L-1: no index division
-        // per element, and the row's v and w are loaded once
-        const int nw = nt >> 5;
-        for (int r = warp; r < L; r += nw) {
+        // warps 1.. one row each, lanes over its columns 1..L-1 (warp 0 is
+        // busy with column 0 and the next reflector): no index division per
+        // element, and the row's v and w are loaded once
+        const int nw = (nt >> 5) - 1;
+        for (int r = warp - 1; warp > 0 && r < L; r += nw) {
           const cx<T> vr = tv[r];
           const cx<T> wr = sm->tp[r] + a2 * vr;
           cx<T>* arow = A + (j + 1 + r) * lda + (j + 1);
@@ -402,7 +414,7 @@ __device__ void tridiagonalize(cx<T>* A, int m, double trace, SmallSmem<T>* sm) 
         }
       } else {
         const int Lc = L - 1;
-        for (int t = tid; t < L * Lc; t += nt) {
+        for (int t = tid - 32; tid >= 32 && t < L * Lc; t += nt - 32) {
           const int r = t / Lc, c = 1 + (t - r * Lc);
           const cx<T> vr = tv[r], vc = tv[c];
           const cx<T> wr = sm->tp[r] + a2 * vr, wc = sm->tp[c] + a2 * vc;
