@@ -365,6 +365,11 @@ int mps_diag_fma_rate(int device, int precision, double* flops_per_s);
  * the bit-for-bit reference of a wider run.  No counterpart in the
  * reference. */
 int mps_diag_set_parallel_width(int max_ctas);
+/* Diagnostic: rows (eigensolver) or columns (QR) per CTA of the wide path's
+ * cooperative launches, process-wide (0 = the default, 8).  More rows per
+ * CTA mean fewer CTAs and cheaper grid barriers, less parallel work per
+ * column.  No counterpart in the reference. */
+int mps_diag_set_coop_rows(int rows_per_cta);
 
 /* Footprint used by admission: sum over sites of chi_l * 2 * chi_r * bytes. */
 size_t mps_footprint_bytes(int n_qubits, int chi_max, int precision);

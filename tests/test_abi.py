@@ -125,7 +125,7 @@ for name, res, argtypes in M.SIGNATURES:
 # or a valid setting
 _NULL_OK = {"mps_ctx_destroy", "mps_program_destroy", "mps_graph_destroy", "mps_serve_stop",
             "mps_autotune_set_mode", "mps_autotune_clear", "mps_diag_set_parallel_width",
-            "mps_gates_many"}
+            "mps_gates_many", "mps_diag_set_coop_rows"}
 
 
 def test_null_arguments_are_errors_not_crashes():

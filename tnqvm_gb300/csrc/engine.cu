@@ -1366,6 +1366,8 @@ int mps_autotune_tunings(mps_ctx* c, int* out) {
   return MPS_OK;
 }
 
+int mps_diag_set_coop_rows(int rows_per_cta) { return wide_set_coop_rows(rows_per_cta); }
+
 int mps_diag_set_parallel_width(int max_ctas) {
   if (max_ctas < 0) return fail(MPS_ERR_ARG, "max_ctas must be >= 0");
   g_parallel_width.store(max_ctas);

@@ -209,6 +209,7 @@ int wide_diag_cgemm(mps_ctx* c, int M, int N, int K, const double* a, const doub
 int wide_diag_cgemm_kind(mps_ctx* c, int prec, int kind, int flags, int M, int N, int K, const double* a,
                          const double* b, double* out);
 int wide_gemm_tunings(mps_ctx* c);
+int wide_set_coop_rows(int rows);
 void wide_free(mps_ctx* c);
 // density programs (density.cu)
 int density_expect(::mps_prog* p, const uint8_t* codes, int n_terms, std::vector<cx<double>>& res);

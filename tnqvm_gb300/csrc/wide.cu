@@ -16,6 +16,7 @@
 // Pauli expectations (ITensorMPSVisitor.cpp:173-250) and shot sampling
 // (ExaTnMpsVisitor.cpp:2211-2364) are transfer-matrix sweeps of GEMMs.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -382,11 +383,14 @@ static int wide_bufs(void** ws, int prec, int chi, WideBufs** out) {
 static int blocks_for(int64_t n) { return (int)std::min<int64_t>((n + 255) / 256, 4096); }
 
 // Grid of a cooperative launch over n rows (eigensolver) or columns (QR):
-// about one per warp, at most the co-resident maximum.  Fewer CTAs make each
-// grid barrier cheaper when the matrix is small.
+// one CTA per g_coop_rows rows (default 8, about one per warp), at most the
+// co-resident maximum.  Fewer CTAs make each grid barrier cheaper when the
+// matrix is small.
+static std::atomic<int> g_coop_rows{8};
 static int coop_grid_for(int prec, int which, int n) {
   const int g = coop_grid(prec, which);
-  const int want = std::max(8, (n + 7) / 8);
+  const int rows = g_coop_rows.load();
+  const int want = std::max(8, (n + rows - 1) / rows);
   return std::min(g, want);
 }
 
@@ -1038,6 +1042,12 @@ int wide_diag_cgemm_kind(mps_ctx* c, int prec, int kind, int flags, int M, int N
                          const double* b, double* out) {
   return prec == MPS_PREC_FP64 ? wide_diag_cgemm_kind_t<double>(c, kind, flags, M, N, K, a, b, out)
                                : wide_diag_cgemm_kind_t<float>(c, kind, flags, M, N, K, a, b, out);
+}
+
+int wide_set_coop_rows(int rows) {
+  if (rows < 0 || rows > 4096) return fail(MPS_ERR_ARG, "rows per CTA must be in 0..4096");
+  g_coop_rows.store(rows == 0 ? 8 : rows);
+  return MPS_OK;
 }
 
 int wide_gemm_tunings(mps_ctx* c) {

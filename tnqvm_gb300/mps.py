@@ -97,6 +97,7 @@ SIGNATURES = [
     ("mps_autotune_tunings", _c.c_int, [_P, _c.POINTER(_c.c_int)]),
     ("mps_channel1", _c.c_int, [_P, _c.c_int, _c.c_int, _DP]),
     ("mps_diag_set_parallel_width", _c.c_int, [_c.c_int]),
+    ("mps_diag_set_coop_rows", _c.c_int, [_c.c_int]),
     ("mps_density_matrix", _c.c_int, [_P, _c.c_int, _c.POINTER(_c.c_int), _DP]),
     ("mps_density_diag", _c.c_int, [_P, _c.c_int, _c.POINTER(_c.c_int), _DP]),
 ]
@@ -280,6 +281,13 @@ def set_parallel_width(max_ctas):
     kernel one op at a time."""
     load_library()
     _check(_lib.mps_diag_set_parallel_width(max_ctas))
+
+
+def set_coop_rows(rows_per_cta):
+    """Rows (or columns) per CTA of the wide path's cooperative launches
+    (0 = the default, 8)."""
+    load_library()
+    _check(_lib.mps_diag_set_coop_rows(rows_per_cta))
 
 
 def autotune_set_mode(mode):
