@@ -746,8 +746,10 @@ def main():
     ap.add_argument("--qmin", type=int, default=8, help="smallest qubit count (small profiling cases)")
     ap.add_argument("--qmax", type=int, default=32, help="largest qubit count (small profiling cases)")
     ap.add_argument("--lmax", type=int, default=12, help="largest layer count (small profiling cases)")
-    ap.add_argument("--leg", default="", choices=["", "qaoa"],
-                    help="run one extra leg alone and print its JSON (qaoa: the 64-qubit precision comparison)")
+    ap.add_argument("--leg", default="", choices=["", "qaoa", "plain", "noisy"],
+                    help="run one extra leg alone and print its JSON (qaoa: the 64-qubit precision comparison; "
+                         "plain: the exatn-mode per-circuit FP64 paths on the stratified sample; noisy: the "
+                         "noisy-circuit leg)")
     ap.add_argument("--qaoa-p", type=int, default=3, help="QAOA rounds of the qaoa leg")
     args = ap.parse_args()
     if args.impl == "reference":
@@ -755,6 +757,20 @@ def main():
     if args.leg == "qaoa":
         build_locked()
         print(json.dumps({"qaoa_precision": qaoa_precision(args)}))
+        return 0
+    if args.leg in ("plain", "noisy"):
+        build_locked()
+        from tnqvm_gb300 import circuits
+        from tnqvm_gb300 import mps as M
+        with M.Context(env_int("LOCAL_RANK", 0)) as ctx:
+            if args.leg == "noisy":
+                print(json.dumps({"noisy": noisy_circuits(ctx)}))
+                return 0
+            insts = circuits.vqe_batch(args.instances, seed=replica_seed(0), qmin=args.qmin, qmax=args.qmax,
+                                       lmax=args.lmax)
+            order = np.argsort([it["n"] * it["layers"] for it in insts])
+            pidx = list(order[:: max(1, len(order) // args.plain_sample)])[: args.plain_sample]
+            print(json.dumps({"plain_fp64_exatn": plain_exatn(args, ctx, [insts[i] for i in pidx], float("nan"))}))
         return 0
     return run_ours(args)
 

@@ -82,6 +82,7 @@ struct ServeReq {
   bool fused = false;
   int* flag = nullptr;       // [0] done, [1] error word
   double* obs = nullptr;     // 2 * (n_terms + 1) doubles
+  size_t exp_off = 0;        // first of its observable results in the batch's pinned buffer
   bool in_batch = false;     // still referenced by a running batch
   bool reaped = false;       // polled by the client while in_batch
 };
@@ -90,7 +91,6 @@ struct ServeBatch {
   int lane;
   std::vector<ServeReq*> reqs;
   cudaEvent_t ev;
-  std::vector<ExpTask> tasks;
   double* h_exp = nullptr;     // pinned, 2 doubles per task
   size_t h_exp_cap = 0;
   std::vector<std::pair<ServeReq*, uint8_t*>> bit_dst;

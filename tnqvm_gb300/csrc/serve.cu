@@ -91,7 +91,6 @@ static void finish_batch(ServeState* S, ServeBatch& B) {
   const double t = now_ms();
   std::atomic_thread_fence(std::memory_order_acquire);
   std::lock_guard<std::mutex> lk(S->mu);
-  size_t ti = 0;
   size_t ri = 0;
   for (ServeReq* r : B.reqs) {
     mps_prog* p = r->prog;
@@ -101,10 +100,7 @@ static void finish_batch(ServeState* S, ServeBatch& B) {
       continue;
     }
     r->status = status_of(herr);
-    if (p->d_obs) {
-      r->energy = observable_value(p, B.h_exp + 2 * ti);
-      ti += (size_t)p->n_terms + 1;
-    }
+    if (p->d_obs) r->energy = observable_value(p, B.h_exp + 2 * r->exp_off);
   }
   for (auto& bd : B.bit_dst) {
     ServeReq* r = bd.first;
@@ -157,15 +153,26 @@ static int launch_batch(mps_ctx* c, ServeState* S, int li, std::vector<ServeReq*
     p->serve_obs = nullptr;
   }
   if (rc) return rc;
-  B.tasks.clear();
-  int prec = progs[0]->prec;
+  // observables of the requests that do not complete on their own CTA: one
+  // expectation launch per precision (a batch may mix complex64 and
+  // complex128 programs), results packed complex128 tasks first
+  std::vector<ExpTask> tasks[2];
   for (ServeReq* r : reqs)
-    if (!r->fused && r->prog->d_obs) observable_tasks(r->prog, B.tasks);
-  if (!B.tasks.empty()) {
-    rc = grow_pinned((void**)&B.h_exp, &B.h_exp_cap, 2 * B.tasks.size() * sizeof(double));
+    if (!r->fused && r->prog->d_obs) {
+      r->exp_off = tasks[r->prog->prec].size();
+      observable_tasks(r->prog, tasks[r->prog->prec]);
+    }
+  const size_t n_tasks = tasks[0].size() + tasks[1].size();
+  if (n_tasks > 0) {
+    rc = grow_pinned((void**)&B.h_exp, &B.h_exp_cap, 2 * n_tasks * sizeof(double));
     if (rc) return rc;
-    rc = enqueue_expect(L, B.tasks, prec, B.h_exp);
-    if (rc) return rc;
+    for (int pr = 0; pr < 2; ++pr) {
+      if (tasks[pr].empty()) continue;
+      rc = enqueue_expect(L, tasks[pr], pr, B.h_exp + (pr == 1 ? 2 * tasks[0].size() : 0));
+      if (rc) return rc;
+    }
+    for (ServeReq* r : reqs)
+      if (!r->fused && r->prog->d_obs && r->prog->prec == 1) r->exp_off += tasks[0].size();
   }
   size_t bit_total = 0;
   for (ServeReq* r : reqs) bit_total += (size_t)r->shots * r->prog->n;
@@ -220,11 +227,11 @@ static void serve_loop(mps_ctx* c) {
       std::unique_lock<std::mutex> lk(S->mu);
       if (S->stop && S->queue.empty() && !any_busy) break;
       if (free_lane >= 0 && !S->queue.empty()) {
-        const int prec = S->queue.front()->prog->prec;
+        // the fused kernel runs each program in its own precision, so a
+        // batch takes every queued request in arrival order
         size_t bytes = S->inflight_bytes;
         while (!S->queue.empty()) {
           ServeReq* r = S->queue.front();
-          if (r->prog->prec != prec) break;
           if (S->inflight_reqs + (int)take.size() >= S->max_inflight) break;
           if (!take.empty() && bytes + r->prog->bytes > c->budget) break;
           bytes += r->prog->bytes;
