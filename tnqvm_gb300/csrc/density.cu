@@ -245,19 +245,11 @@ int density_expect(mps_prog* p, const uint8_t* codes, int n_terms, std::vector<c
   return rc;
 }
 
-}  // namespace gbmps
-
-using namespace gbmps;
-
-extern "C" {
-
-int mps_channel1(mps_prog* p, int qubit, int n_kraus, const double* kraus) {
-  if (!p || !kraus || n_kraus < 1) return fail(MPS_ERR_ARG, "bad argument");
-  if (!p->density) return fail(MPS_ERR_STATE, "channels need a program begun with MPS_FLAG_DENSITY");
-  if (qubit < 0 || qubit >= p->nq) return fail(MPS_ERR_ARG, "qubit index out of range");
-  // S[(2i + j)][(2i' + j')] = sum_k K[i][i'] conj(K[j][j']): rows and columns
-  // are 2 * phys(ket site) + phys(bra site), the ket site the lower one
-  GateRec g;
+// The superoperator of rho -> sum_k K_k rho K_k^H on the adjacent sites
+// (2q, 2q+1): S[(2i + j)][(2i' + j')] = sum_k K[i][i'] conj(K[j][j']), rows and
+// columns 2 * phys(ket site) + phys(bra site) with the ket site the lower one.
+// kraus: n_kraus 2x2 matrices, row-major (re, im) pairs.
+int kraus_superop(int qubit, int n_kraus, const double* kraus, GateRec& g) {
   g.nq = 2;
   g.q0 = 2 * qubit;
   g.q1 = 2 * qubit + 1;
@@ -275,6 +267,22 @@ int mps_channel1(mps_prog* p, int qubit, int n_kraus, const double* kraus) {
   }
   for (int i = 0; i < 16; ++i)
     if (!std::isfinite(g.m[i].real()) || !std::isfinite(g.m[i].imag())) return fail(MPS_ERR_ARG, "non-finite Kraus entry");
+  return MPS_OK;
+}
+
+}  // namespace gbmps
+
+using namespace gbmps;
+
+extern "C" {
+
+int mps_channel1(mps_prog* p, int qubit, int n_kraus, const double* kraus) {
+  if (!p || !kraus || n_kraus < 1) return fail(MPS_ERR_ARG, "bad argument");
+  if (!p->density) return fail(MPS_ERR_STATE, "channels need a program begun with MPS_FLAG_DENSITY");
+  if (qubit < 0 || qubit >= p->nq) return fail(MPS_ERR_ARG, "qubit index out of range");
+  GateRec g;
+  const int rc = kraus_superop(qubit, n_kraus, kraus, g);
+  if (rc) return rc;
   p->pending.push_back(g);
   return MPS_OK;
 }

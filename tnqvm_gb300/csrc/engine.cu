@@ -641,6 +641,26 @@ double observable_value(const mps_prog* p, const double* r) {
   return nrm > 0.0 ? e / nrm : 0.0;
 }
 
+// Record a gate on qubits; a density program applies U to the ket sites and
+// conj(U) to the bra sites: rho -> U rho U^H.
+void record_gate(mps_prog* p, const GateRec& g) {
+  if (!p->density) {
+    p->pending.push_back(g);
+    return;
+  }
+  GateRec k = g, b = g;
+  k.q0 = 2 * g.q0;
+  b.q0 = 2 * g.q0 + 1;
+  if (g.nq == 2) {
+    k.q1 = 2 * g.q1;
+    b.q1 = 2 * g.q1 + 1;
+  }
+  const int ne = g.nq == 2 ? 16 : 4;
+  for (int i = 0; i < ne; ++i) b.m[i] = std::conj(g.m[i]);
+  p->pending.push_back(k);
+  p->pending.push_back(b);
+}
+
 }  // namespace gbmps
 
 using namespace gbmps;
@@ -854,26 +874,6 @@ static int check_q(mps_prog* p, int q) {
   return MPS_OK;
 }
 
-// Record a gate on qubits; a density program applies U to the ket sites and
-// conj(U) to the bra sites: rho -> U rho U^H.
-static void push_gate(mps_prog* p, const GateRec& g) {
-  if (!p->density) {
-    p->pending.push_back(g);
-    return;
-  }
-  GateRec k = g, b = g;
-  k.q0 = 2 * g.q0;
-  b.q0 = 2 * g.q0 + 1;
-  if (g.nq == 2) {
-    k.q1 = 2 * g.q1;
-    b.q1 = 2 * g.q1 + 1;
-  }
-  const int ne = g.nq == 2 ? 16 : 4;
-  for (int i = 0; i < ne; ++i) b.m[i] = std::conj(g.m[i]);
-  p->pending.push_back(k);
-  p->pending.push_back(b);
-}
-
 int mps_gate1(mps_prog* p, int q, const double m[8]) {
   if (!p || !m) return fail(MPS_ERR_ARG, "NULL argument");
   if (check_q(p, q)) return MPS_ERR_ARG;
@@ -882,7 +882,7 @@ int mps_gate1(mps_prog* p, int q, const double m[8]) {
   g.q0 = q;
   g.q1 = -1;
   for (int i = 0; i < 4; ++i) g.m[i] = cd(m[2 * i], m[2 * i + 1]);
-  push_gate(p, g);
+  record_gate(p, g);
   return MPS_OK;
 }
 
@@ -895,7 +895,7 @@ int mps_gate2(mps_prog* p, int q0, int q1, const double m[32]) {
   g.q0 = q0;
   g.q1 = q1;
   for (int i = 0; i < 16; ++i) g.m[i] = cd(m[2 * i], m[2 * i + 1]);
-  push_gate(p, g);
+  record_gate(p, g);
   return MPS_OK;
 }
 
@@ -927,7 +927,7 @@ int mps_gate_named(mps_prog* p, const char* name, const int* qubits, int nq, con
   g.q0 = qubits[0];
   g.q1 = k == 2 ? qubits[1] : -1;
   if (k == 2 && g.q0 == g.q1) return fail(MPS_ERR_ARG, "two-qubit gate on one qubit");
-  push_gate(p, g);
+  record_gate(p, g);
   return MPS_OK;
 }
 

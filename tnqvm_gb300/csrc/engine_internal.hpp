@@ -211,7 +211,10 @@ int wide_diag_cgemm_kind(mps_ctx* c, int prec, int kind, int flags, int M, int N
 int wide_gemm_tunings(mps_ctx* c);
 int wide_set_coop_rows(int rows);
 void wide_free(mps_ctx* c);
-// density programs (density.cu)
+// density programs: a gate recorded on qubits (engine.cu), a single-qubit
+// Kraus channel as the two-site superoperator on (2q, 2q+1) (density.cu)
+void record_gate(::mps_prog* p, const GateRec& g);
+int kraus_superop(int qubit, int n_kraus, const double* kraus, GateRec& g);
 int density_expect(::mps_prog* p, const uint8_t* codes, int n_terms, std::vector<cx<double>>& res);
 int density_sample(::mps_prog* p, int shots, uint64_t seed, uint8_t* bits);
 }  // namespace gbmps
