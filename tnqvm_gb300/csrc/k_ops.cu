@@ -519,8 +519,13 @@ __device__ void tri_multisect(int m, SmallSmem<T>* sm, int rounds) {
       if (__shfl_sync(gmask, cnt, base + u) > local) first = u;
     const T na = first == 0 ? a : a + w * T(first);
     const T nb = first == L ? b : a + w * T(first + 1);
+    // a bracket that no longer moves never moves again (the same points,
+    // the same counts): the warp stops once all of its brackets are stuck,
+    // with the results of the full round count
+    const bool stuck = !live || (na == a && nb == b);
     a = na;
     b = nb;
+    if (__all_sync(0xffffffffu, stuck)) break;
   }
   if (live && q == 0) sm->lam[j] = T(0.5) * (a + b);
 }
