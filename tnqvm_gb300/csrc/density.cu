@@ -150,15 +150,16 @@ static int dm_contract(mps_prog* p, const std::vector<int>& sel, int64_t W0, con
   cudaError_t e = cudaMemcpyAsync(bond.data(), p->d_bond, bond.size() * sizeof(int), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return fail(MPS_ERR_CUDA, cudaGetErrorString(e));
-  int64_t W = W0, Wmax = W0;
-  int bmax = 1;
-  for (int b : bond) bmax = std::max(bmax, b);
+  // largest vector of the walk: the ket step's (bond x 2W) or the bra
+  // step's (bond x W'), where W grows with the open indices so far
+  int64_t W = W0;
+  size_t elems = (size_t)W0;
   for (int q = 0; q < nq; ++q) {
-    if (sel[q] == DM_DIAG) W *= 2;
-    if (sel[q] == DM_FULL) W *= 4;
-    Wmax = std::max(Wmax, W);
+    const int64_t wo = sel[q] == DM_DIAG ? 2 * W : (sel[q] == DM_FULL ? 4 * W : W);
+    elems = std::max(elems, (size_t)bond[2 * q + 1] * 2 * (size_t)W);
+    elems = std::max(elems, (size_t)bond[2 * q + 2] * (size_t)wo);
+    W = wo;
   }
-  const size_t elems = (size_t)bmax * 2 * (size_t)Wmax;
   if (3 * elems * sizeof(cx<double>) > kDmWorkBytes)
     return fail(MPS_ERR_UNSUPPORTED, "density-matrix contraction too large for the work buffers");
   cx<double>* buf = nullptr;

@@ -49,9 +49,10 @@ static int grow_pinned(void** p, size_t* cap, size_t need) {
 }
 
 static int status_of(int herr) {
-  return (herr & ERR_NAN)    ? fail(MPS_ERR_NUMERIC, "non-finite value in a two-site split")
-         : (herr & ERR_DIMS) ? fail(MPS_ERR_UNSUPPORTED, "bond dimension beyond the kernel limit")
-                             : MPS_OK;
+  return (herr & ERR_NAN)       ? fail(MPS_ERR_NUMERIC, "non-finite value in a two-site split")
+         : (herr & ERR_DIMS)    ? fail(MPS_ERR_UNSUPPORTED, "bond dimension beyond the kernel limit")
+         : (herr & ERR_TIMEOUT) ? fail(MPS_ERR_TIMEOUT, "a site-parallel update waited past its bound")
+                                : MPS_OK;
 }
 
 // Completion bookkeeping of one request (S->mu held).
