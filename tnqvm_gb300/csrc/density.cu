@@ -126,9 +126,10 @@ __global__ void k_dm_bra(const cx<T>* __restrict__ B, int dm, int dr, int64_t W,
   }
 }
 
-static int grid_for(int64_t total) {
+// One thread per output, grid-stride beyond 32 CTAs per SM.
+static int grid_for(int64_t total, int sms) {
   int64_t g = (total + 255) / 256;
-  if (g > 152 * 32) g = 152 * 32;
+  if (g > (int64_t)sms * 32) g = (int64_t)sms * 32;
   if (g < 1) g = 1;
   return (int)g;
 }
@@ -182,17 +183,17 @@ static int dm_contract(mps_prog* p, const std::vector<int>& sel, int64_t W0, con
     const char* B = (const char*)p->d_sites + p->off[s1] * eb;
     const int64_t tk = (int64_t)dm * 2 * W;
     if (p->prec == MPS_PREC_FP64)
-      k_dm_ket<double><<<grid_for(tk), 256, 0, st>>>((const cx<double>*)A, dl, dm, W, vin, U);
+      k_dm_ket<double><<<grid_for(tk, c->num_sms), 256, 0, st>>>((const cx<double>*)A, dl, dm, W, vin, U);
     else
-      k_dm_ket<float><<<grid_for(tk), 256, 0, st>>>((const cx<float>*)A, dl, dm, W, vin, U);
+      k_dm_ket<float><<<grid_for(tk, c->num_sms), 256, 0, st>>>((const cx<float>*)A, dl, dm, W, vin, U);
     const int mode = sel[q];
     const int64_t wo = mode == DM_CLOSE ? W : (mode == DM_DIAG ? 2 * W : 4 * W);
     const uint8_t* cq = (mode == DM_CLOSE && d_codes) ? d_codes + q : nullptr;
     if (p->prec == MPS_PREC_FP64)
-      k_dm_bra<double><<<grid_for((int64_t)dr * wo), 256, 0, st>>>((const cx<double>*)B, dm, dr, W, U, mode, cq,
+      k_dm_bra<double><<<grid_for((int64_t)dr * wo, c->num_sms), 256, 0, st>>>((const cx<double>*)B, dm, dr, W, U, mode, cq,
                                                                    stride, n_codes, vout);
     else
-      k_dm_bra<float><<<grid_for((int64_t)dr * wo), 256, 0, st>>>((const cx<float>*)B, dm, dr, W, U, mode, cq,
+      k_dm_bra<float><<<grid_for((int64_t)dr * wo, c->num_sms), 256, 0, st>>>((const cx<float>*)B, dm, dr, W, U, mode, cq,
                                                                   stride, n_codes, vout);
     e = cudaGetLastError();
     std::swap(vin, vout);
@@ -387,6 +388,7 @@ int density_sample(mps_prog* p, int shots, uint64_t seed, uint8_t* bits) {
   }
   if (!(acc > 0.0)) return fail(MPS_ERR_NUMERIC, "density matrix with no positive diagonal");
   for (int s = 0; s < shots; ++s) {
+    // one uniform per shot (counter = shot), on a stream tag of its own
     const double u = philox_uniform(seed, (uint32_t)s, 0u, 0x5D3A7u) * acc;
     size_t k = std::upper_bound(cdf.begin(), cdf.end(), u) - cdf.begin();
     if (k >= cdf.size()) k = cdf.size() - 1;
