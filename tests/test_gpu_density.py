@@ -233,3 +233,25 @@ def test_density_errors(ctx):
             M.Graph(ctx, [p])
         assert e.value.code == M.ERR_UNSUPPORTED
         assert abs(p.norm() - 1.0) < 1e-12
+
+
+@pytest.mark.parametrize("mode", [M.TRUNC_EXATN, M.TRUNC_ITENSOR])
+def test_density_site_parallel_equals_one_op_at_a_time(ctx, mode):
+    """Density programs run site-parallel (the noisy visitor's default): the
+    same density matrix, bit for bit, as the same kernel one op at a time."""
+    rng = np.random.default_rng(55)
+    n = 5
+    circ = _random_circuit(n, 5, rng)
+    outs = []
+    for width in (1, 0):
+        M.set_parallel_width(width)
+        try:
+            with M.DensityProgram(ctx, n, 16, 1e-12, mode, M.PREC_FP64, M.FLAG_PARALLEL) as p:
+                record(p, circ)
+                p.submit()
+                p.wait()
+                outs.append((p.density_matrix(range(n)), p.bond_dims()))
+        finally:
+            M.set_parallel_width(0)
+    assert outs[0][1] == outs[1][1]
+    assert np.array_equal(outs[0][0], outs[1][0])

@@ -256,7 +256,8 @@ class GpuPmpsVisitor:
     format; the reference reads an IBM backend description there, which
     needs XACC's IBM noise model), ``shots`` (default 1024, ``:539``),
     ``seed``, ``max-bond-dim``, ``svd-cutoff``, ``precision``,
-    ``truncation-mode``."""
+    ``truncation-mode``, ``parallel`` (default on: independent two-site
+    updates of the doubled chain on different SMs, same results)."""
 
     def __init__(self, ctx=None):
         self.ctx = ctx
@@ -303,7 +304,10 @@ class GpuPmpsVisitor:
         self.buffer = buffer
         # a noisy simulation always runs shots (:539)
         self.shots = 1024 if nbShots < 1 else nbShots
-        self.prog = M.DensityProgram(self.ctx, buffer.size(), chi, cutoff, mode, prec)
+        # the ket and bra halves of a gate, and gates on disjoint qubits, run on
+        # different SMs at once (same results)
+        flags = M.FLAG_PARALLEL if o.get("parallel", True) else 0
+        self.prog = M.DensityProgram(self.ctx, buffer.size(), chi, cutoff, mode, prec, flags)
         self.measured = []
 
     def visit(self, name, qubits, params=()):

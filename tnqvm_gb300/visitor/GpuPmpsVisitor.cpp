@@ -44,8 +44,11 @@ void GpuPmpsVisitor::initialize(std::shared_ptr<AcceleratorBuffer> in_buffer, in
   measured_.clear();
   if (prog_) mps_program_destroy(prog_);
   prog_ = nullptr;
-  check(mps_program_begin(gb300_context(), (int)buffer->size(), chi, cutoff, mode, prec, MPS_FLAG_DENSITY,
-                          &prog_),
+  // the ket and bra halves of a gate, and gates on disjoint qubits, run on
+  // different SMs at once (same results); "parallel" false turns it off
+  int flags = MPS_FLAG_DENSITY;
+  if (!(options.keyExists<bool>("parallel") && !options.get<bool>("parallel"))) flags |= MPS_FLAG_PARALLEL;
+  check(mps_program_begin(gb300_context(), (int)buffer->size(), chi, cutoff, mode, prec, flags, &prog_),
         "initialize");
 }
 
