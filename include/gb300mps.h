@@ -152,8 +152,9 @@ int mps_gates(mps_prog* p, int n_gates, const int32_t* ids, const int32_t* qubit
 /* The same for many programs in one call (e.g. new parameters for every
  * circuit of a batch): program i records gates first_gate[i] ..
  * first_gate[i+1]-1 of the concatenated arrays (first_gate has n_progs+1
- * entries); programs are recorded on host threads.  On failure the first
- * failing program is reported and the others have recorded their gates. */
+ * entries); programs are recorded on host threads, so each may appear only
+ * once (MPS_ERR_ARG otherwise).  On failure the first failing program is
+ * reported and the others have recorded their gates. */
 int mps_gates_many(int n_progs, mps_prog* const* progs, const int64_t* first_gate, const int32_t* ids,
                    const int32_t* qubits, const double* params);
 

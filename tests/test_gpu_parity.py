@@ -536,6 +536,10 @@ def test_batch_record_equals_per_program_record(ctx):
             p.set_observable(it["paulis"], it["coeffs"])
             q.set_observable(it["paulis"], it["coeffs"])
         assert np.array_equal(ctx.batch_expect(a), ctx.batch_expect(b))
+        # one program listed twice would be recorded by two threads at once
+        with pytest.raises(M.MpsError) as e:
+            M.BatchRecord([a[0], a[0]], [encs[0], encs[0]]).record()
+        assert e.value.code == M.ERR_ARG
     finally:
         for p in a + b:
             p.close()

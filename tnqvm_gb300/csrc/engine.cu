@@ -956,6 +956,14 @@ int mps_gates_many(int n_progs, mps_prog* const* progs, const int64_t* first_gat
     if (first_gate[i + 1] < first_gate[i] || first_gate[i + 1] - first_gate[i] > INT32_MAX)
       return fail(MPS_ERR_ARG, "first_gate must be non-decreasing");
   }
+  {
+    // each program is recorded by one thread: a program listed twice would be
+    // written by two
+    std::vector<mps_prog*> sorted(progs, progs + n_progs);
+    std::sort(sorted.begin(), sorted.end());
+    if (std::adjacent_find(sorted.begin(), sorted.end()) != sorted.end())
+      return fail(MPS_ERR_ARG, "a program is listed twice");
+  }
   // programs record independently: host threads, the first failure (lowest
   // program index) is reported
   std::vector<int> rcs(n_progs, MPS_OK);
