@@ -181,20 +181,19 @@ static int dm_contract(mps_prog* p, const std::vector<int>& sel, int64_t W0, con
     const int dl = bond[s0], dm = bond[s0 + 1], dr = bond[s1 + 1];
     const char* A = (const char*)p->d_sites + p->off[s0] * eb;
     const char* B = (const char*)p->d_sites + p->off[s1] * eb;
-    const int64_t tk = (int64_t)dm * 2 * W;
+    const int gk = grid_for((int64_t)dm * 2 * W, c->num_sms);
     if (p->prec == MPS_PREC_FP64)
-      k_dm_ket<double><<<grid_for(tk, c->num_sms), 256, 0, st>>>((const cx<double>*)A, dl, dm, W, vin, U);
+      k_dm_ket<double><<<gk, 256, 0, st>>>((const cx<double>*)A, dl, dm, W, vin, U);
     else
-      k_dm_ket<float><<<grid_for(tk, c->num_sms), 256, 0, st>>>((const cx<float>*)A, dl, dm, W, vin, U);
+      k_dm_ket<float><<<gk, 256, 0, st>>>((const cx<float>*)A, dl, dm, W, vin, U);
     const int mode = sel[q];
     const int64_t wo = mode == DM_CLOSE ? W : (mode == DM_DIAG ? 2 * W : 4 * W);
     const uint8_t* cq = (mode == DM_CLOSE && d_codes) ? d_codes + q : nullptr;
+    const int gb = grid_for((int64_t)dr * wo, c->num_sms);
     if (p->prec == MPS_PREC_FP64)
-      k_dm_bra<double><<<grid_for((int64_t)dr * wo, c->num_sms), 256, 0, st>>>((const cx<double>*)B, dm, dr, W, U, mode, cq,
-                                                                   stride, n_codes, vout);
+      k_dm_bra<double><<<gb, 256, 0, st>>>((const cx<double>*)B, dm, dr, W, U, mode, cq, stride, n_codes, vout);
     else
-      k_dm_bra<float><<<grid_for((int64_t)dr * wo, c->num_sms), 256, 0, st>>>((const cx<float>*)B, dm, dr, W, U, mode, cq,
-                                                                  stride, n_codes, vout);
+      k_dm_bra<float><<<gb, 256, 0, st>>>((const cx<float>*)B, dm, dr, W, U, mode, cq, stride, n_codes, vout);
     e = cudaGetLastError();
     std::swap(vin, vout);
     W = wo;
