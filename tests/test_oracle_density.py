@@ -212,3 +212,21 @@ def test_product_json_model_reads_like_the_oracle():
             for x, y in zip(ca, cb):
                 assert np.array_equal(np.array(x), np.array(y))
         assert a.readout_error(0) == b.readout.get(0, (0.0, 0.0))
+
+
+def test_product_json_model_lookup_rules():
+    """The product's JSON noise model: channels by gate name (CX and CNOT
+    alike) and exact qubit list, none for other gates or qubits, readout
+    (0, 0) for a qubit the model does not list."""
+    from tnqvm_gb300.noise import JsonNoiseModel
+    k = [[[1, 0], [0, 0]], [[0, 0], [0, 1]]]
+    doc = {"gate_noise": [{"gate_name": "CX", "register_location": ["1", "2"], "noise_channels": [{"matrix": [
+        [[[1, 0], [0, 0]], [[0, 0], [1, 0]]]]}]},
+                          {"gate_name": "H", "register_location": ["0"], "noise_channels": [{"matrix": [k]}]}],
+           "readout_errors": [{"register_location": "3", "prob_meas0_prep1": 0.25, "prob_meas1_prep0": 0.5}]}
+    m = JsonNoiseModel(doc)
+    assert len(m.channels("CNOT", [1, 2])) == 1 and len(m.channels("CX", [1, 2])) == 1
+    assert m.channels("CNOT", [2, 1]) == [] and m.channels("H", [1]) == [] and m.channels("X", [0]) == []
+    q, mats = m.channels("H", [0])[0]
+    assert q == [0] and len(mats) == 1 and mats[0].shape == (2, 2)
+    assert m.readout_error(3) == (0.25, 0.5) and m.readout_error(0) == (0.0, 0.0)
