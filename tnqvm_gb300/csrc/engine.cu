@@ -437,37 +437,14 @@ int launch_programs(mps_ctx* c, Lane& L, mps_prog* const* progs_in, int n_in, bo
       }
     } else if (n == 1 && nd == 1 && (progs[0]->flags & MPS_FLAG_PARALLEL) && progs[0]->serve_flag == nullptr &&
                flat.size() > 1) {
-      // site-parallel.  Ops are handed out by level (1 + the level of the
-      // previous op on each of their sites), program order within a level:
-      // ops of one level are independent, so the CTAs claiming them run at
-      // once instead of queueing behind a chain, and every site still sees
-      // its ops in program order (a later op on a site has a higher level).
-      // Per op: the number of earlier ops on each of its sites.
+      // site-parallel: the ops by dependency level, with per-op counts of
+      // earlier ops on their sites, then the op counter and per-site counts
       const mps_prog* p = progs[0];
       const size_t nops = flat.size();
-      std::vector<int> level(nops), last(p->n, 0);
-      for (size_t o = 0; o < nops; ++o) {
-        const DevOp& op = flat[o];
-        const int s0 = op.kind == OP_MOVE_L ? op.site - 1 : op.site;
-        const bool two = op.kind != OP_GATE1;
-        const int l = 1 + std::max(last[s0], two ? last[s0 + 1] : 0);
-        level[o] = l;
-        last[s0] = l;
-        if (two) last[s0 + 1] = l;
-      }
-      std::vector<int> order(nops);
-      for (size_t o = 0; o < nops; ++o) order[o] = (int)o;
-      std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return level[a] < level[b]; });
-      std::vector<DevOp> sorted(nops);
-      std::vector<int> host((nops * 2) + 1 + p->n, 0);
-      std::vector<int> seen(p->n, 0);
-      for (size_t k = 0; k < nops; ++k) {
-        const DevOp& op = flat[order[k]];
-        sorted[k] = op;
-        const int s0 = op.kind == OP_MOVE_L ? op.site - 1 : op.site;
-        host[2 * k] = seen[s0]++;
-        host[2 * k + 1] = op.kind == OP_GATE1 ? -1 : seen[s0 + 1]++;
-      }
+      std::vector<DevOp> sorted;
+      std::vector<int> host;
+      site_schedule(flat, p->n, sorted, host);
+      host.resize(nops * 2 + 1 + p->n, 0);
       // pageable source: staged before the call returns; lands over the
       // program-order table uploaded above
       e = cudaMemcpyAsync(L.d_ops, sorted.data(), nops * sizeof(DevOp), cudaMemcpyHostToDevice, L.stream);
@@ -639,6 +616,40 @@ double observable_value(const mps_prog* p, const double* r) {
   double e = 0.0;
   for (int t = 0; t < p->n_terms; ++t) e += p->obs_coef[t] * r[2 * (size_t)t];
   return nrm > 0.0 ? e / nrm : 0.0;
+}
+
+// Schedule of a site-parallel run.  Ops are handed out by level (1 + the
+// level of the previous op on each of their sites), program order within a
+// level: ops of one level are independent, so the CTAs claiming them run at
+// once instead of queueing behind a chain, and every site still sees its ops
+// in program order (a later op on a site has a higher level).  deps holds,
+// per op of the sorted list, the number of earlier ops on its first and
+// second site (-1 for a one-site op).
+void site_schedule(const std::vector<DevOp>& ops, int n_sites, std::vector<DevOp>& sorted, std::vector<int>& deps) {
+  const size_t nops = ops.size();
+  std::vector<int> level(nops), last(n_sites, 0);
+  for (size_t o = 0; o < nops; ++o) {
+    const DevOp& op = ops[o];
+    const int s0 = op.kind == OP_MOVE_L ? op.site - 1 : op.site;
+    const bool two = op.kind != OP_GATE1;
+    const int l = 1 + std::max(last[s0], two ? last[s0 + 1] : 0);
+    level[o] = l;
+    last[s0] = l;
+    if (two) last[s0 + 1] = l;
+  }
+  std::vector<int> order(nops);
+  for (size_t o = 0; o < nops; ++o) order[o] = (int)o;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return level[a] < level[b]; });
+  sorted.resize(nops);
+  deps.assign(2 * nops, 0);
+  std::vector<int> seen(n_sites, 0);
+  for (size_t k = 0; k < nops; ++k) {
+    const DevOp& op = ops[order[k]];
+    sorted[k] = op;
+    const int s0 = op.kind == OP_MOVE_L ? op.site - 1 : op.site;
+    deps[2 * k] = seen[s0]++;
+    deps[2 * k + 1] = op.kind == OP_GATE1 ? -1 : seen[s0 + 1]++;
+  }
 }
 
 // Record a gate on qubits; a density program applies U to the ket sites and

@@ -181,6 +181,7 @@ extern thread_local std::string g_err;
 int fail(int code, const std::string& msg);
 size_t footprint(int n, int chi, int prec);
 void compile_program(::mps_prog* p, std::vector<DevOp>& ops);
+void site_schedule(const std::vector<DevOp>& ops, int n_sites, std::vector<DevOp>& sorted, std::vector<int>& deps);
 int lane_init(Lane& L, int priority = 0);
 void lane_free(Lane& L);
 int launch_programs(mps_ctx* c, Lane& L, ::mps_prog* const* progs, int n, bool per_gate);
