@@ -255,3 +255,27 @@ def test_density_site_parallel_equals_one_op_at_a_time(ctx, mode):
             M.set_parallel_width(0)
     assert outs[0][1] == outs[1][1]
     assert np.array_equal(outs[0][0], outs[1][0])
+
+
+def test_pmps_visitor_ibm_backend_reference_checks(ctx):
+    """The reference's IBM-backend noise tests through the noisy visitor with
+    the ibmqx2 description as ``backend-json`` (NoiseModelTester.cpp
+    checkReadout, checkGateTime, checkGateError; ExaTnPmpsTester.cpp
+    checkSimple, checkMultipleQubits, checkBell), 8192 shots each, at the
+    tests' own tolerances."""
+    backend = json.load(open(os.path.join(HERE, "golden", "ibmqx2_backend.json")))["backend"]
+    text = json.dumps(backend)
+
+    def p(n, circ, key, seed):
+        buf = _visitor(ctx, n, circ, {"backend-json": text, "seed": seed}, shots=8192)
+        return buf.computeMeasurementProbability(key)
+
+    m0, m1, m2 = ("Measure", [0], ()), ("Measure", [1], ()), ("Measure", [2], ())
+    x = ("X", [0], ())
+    assert abs(p(1, [m0], "1", 1) - 0.0154) < 0.01
+    hzh = [("H", [0], ()), ("Z", [0], ()), ("H", [0], ()), m0]
+    assert abs(p(1, [x, m0], "1", 2) - p(1, hzh, "1", 3)) < 0.01
+    assert p(1, [x] * 200 + [m0], "1", 4) > 0.1
+    assert p(1, [x] * 100 + [m0], "1", 5) > 0.01
+    assert 0.8 < p(3, [("X", [0], ()), ("X", [1], ()), ("X", [2], ()), m0, m1, m2], "111", 6) < 0.99
+    assert 0.8 < p(2, [x, ("CNOT", [0, 1], ()), m0, m1], "11", 7) < 0.99

@@ -230,3 +230,62 @@ def test_product_json_model_lookup_rules():
     q, mats = m.channels("H", [0])[0]
     assert q == [0] and len(mats) == 1 and mats[0].shape == (2, 2)
     assert m.readout_error(3) == (0.25, 0.5) and m.readout_error(0) == (0.0, 0.0)
+
+
+BACKEND = json.load(open(os.path.join(HERE, "golden", "ibmqx2_backend.json")))
+
+
+def _oracle_noise(model):
+    class Adapter:
+        def channels(self, name, qs):
+            return [(q[0], k) for q, k in model.channels(name, qs) if len(q) == 1]
+    return Adapter()
+
+
+def test_backend_model_channels():
+    """The device model's channels are trace preserving; relaxation for time t
+    decays the excited population by exp(-t/T1) and coherences by exp(-t/T2);
+    relaxation plus depolarizing has the gate's reported average error."""
+    from tnqvm_gb300 import noise as N
+    m = N.BackendNoiseModel(BACKEND["backend"])
+    for name, qs in (("X", [0]), ("H", [2]), ("Ry", [1]), ("CNOT", [0, 1]), ("CZ", [3, 4]), ("I", [4])):
+        for q, kraus in m.channels(name, qs):
+            assert np.allclose(sum(k.conj().T @ k for k in kraus), np.eye(2), atol=1e-12), (name, q)
+    t, t1, t2 = 500.0, 40e3, 30e3
+    k = N.thermal_relaxation_kraus(t, t1, t2)
+    rho = np.array([[0.3, 0.2 + 0.1j], [0.2 - 0.1j, 0.7]])
+    out = sum(x @ rho @ x.conj().T for x in k)
+    assert abs(out[1, 1] - 0.7 * np.exp(-t / t1)) < 1e-14
+    assert abs(out[0, 1] - rho[0, 1] * np.exp(-t / t2)) < 1e-14
+    props = {(g["gate"], tuple(g["qubits"])): {p["name"]: p["value"] for p in g["parameters"]}
+             for g in BACKEND["backend"]["gates"]}
+    err = props[("x", (0,))]["gate_error"]
+    chans = m.channels("X", [0])
+    # compose relaxation then depolarizing: process fidelity -> average gate fidelity
+    comp = [d @ r for d in chans[1][1] for r in chans[0][1]]
+    f_avg = (2 * N.process_fidelity(comp) + 1) / 3
+    assert abs((1 - f_avg) - err) < 1e-12
+    assert m.channels("Rz", [0]) == [] and m.channels("Z", [1]) == []
+
+
+def test_backend_model_reproduces_reference_checks():
+    """The checks of the reference's IBM-backend tests on the dense oracle
+    with the device model (NoiseModelTester.cpp, ExaTnPmpsTester.cpp):
+    readout P(1|0) = 0.0154 +- 0.01, X against H Z H within 0.01, 100 X
+    gives P(1) > 0.01, 200 X P(1) > 0.1, X on three qubits 0.8 < P(111) <
+    0.99, a Bell pair 0.8 < P(11) < 0.99."""
+    from tnqvm_gb300 import noise as N
+    m = N.BackendNoiseModel(BACKEND["backend"])
+    adapter = _oracle_noise(m)
+
+    def probs(circ, n, meas):
+        rho = R.run(n, circ, noise=adapter)
+        return R.readout_probabilities(R.probabilities(rho, n, meas), meas, {q: m.readout_error(q) for q in meas})
+
+    x = ("X", [0], ())
+    assert abs(probs([], 1, [0])[1] - 0.0154) < 0.01
+    assert abs(probs([x], 1, [0])[1] - probs([("H", [0], ()), ("Z", [0], ()), ("H", [0], ())], 1, [0])[1]) < 0.01
+    assert probs([x] * 100, 1, [0])[1] > 0.01
+    assert probs([x] * 200, 1, [0])[1] > 0.1
+    assert 0.8 < probs([("X", [0], ()), ("X", [1], ()), ("X", [2], ())], 3, [0, 1, 2])[7] < 0.99
+    assert 0.8 < probs([x, ("CNOT", [0, 1], ())], 2, [0, 1])[3] < 0.99

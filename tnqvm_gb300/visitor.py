@@ -252,9 +252,9 @@ class GpuPmpsVisitor:
     (``applySingleQubitGate`` / ``applyTwoQubitGate`` ``:820-885``).
 
     Options: ``noise-model`` (a ``JsonNoiseModel``, any object with its two
-    methods, or the JSON text), ``backend-json`` (JSON text of the same
-    format; the reference reads an IBM backend description there, which
-    needs XACC's IBM noise model), ``shots`` (default 1024, ``:539``),
+    methods, or the JSON text), ``backend-json`` (an IBM backend
+    description: ``BackendNoiseModel``, thermal relaxation and depolarizing
+    noise from its qubit and gate properties), ``shots`` (default 1024, ``:539``),
     ``seed``, ``max-bond-dim``, ``svd-cutoff``, ``precision``,
     ``truncation-mode``, ``parallel`` (default on: independent two-site
     updates of the doubled chain on different SMs, same results)."""
@@ -287,13 +287,15 @@ class GpuPmpsVisitor:
 
     def initialize(self, buffer, nbShots=1):
         """ExaTnPmpsVisitor::initialize (:482-542)."""
-        from .noise import JsonNoiseModel
+        from .noise import BackendNoiseModel, JsonNoiseModel
         if self.ctx is None:
             self.ctx = default_context()
         o = self.options
-        nm = o.get("noise-model", o.get("backend-json"))
+        nm = o.get("noise-model")
         if isinstance(nm, (str, bytes)):
             nm = JsonNoiseModel(nm)
+        if nm is None and "backend-json" in o:
+            nm = BackendNoiseModel(o["backend-json"])
         self.noise = nm
         mode = {"exatn": M.TRUNC_EXATN, "itensor": M.TRUNC_ITENSOR}[o.get("truncation-mode", "exatn")]
         prec = {"fp64": M.PREC_FP64, "fp32": M.PREC_FP32}[o.get("precision", "fp64")]
