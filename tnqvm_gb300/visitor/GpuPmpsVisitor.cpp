@@ -36,8 +36,25 @@ void GpuPmpsVisitor::initialize(std::shared_ptr<AcceleratorBuffer> in_buffer, in
   if (options.keyExists<std::string>("precision") && options.get<std::string>("precision") == "fp32")
     prec = MPS_PREC_FP32;
   noise_.reset();
+#ifdef GB300MPS_WITH_XACC
+  // as ExaTnPmpsVisitor::initialize (:518-536): a NoiseModel object, or the
+  // IBM noise-model service initialised from a backend description or name
+  if (options.pointerLikeExists<xacc::NoiseModel>("noise-model")) {
+    noise_ = xacc::as_shared_ptr(options.getPointerLike<xacc::NoiseModel>("noise-model"));
+  } else {
+    if (options.stringExists("backend-json")) {
+      noise_ = xacc::getService<xacc::NoiseModel>("IBM");
+      noise_->initialize({{"backend-json", options.getString("backend-json")}});
+    }
+    if (options.stringExists("backend")) {
+      noise_ = xacc::getService<xacc::NoiseModel>("IBM");
+      noise_->initialize({{"backend", options.getString("backend")}});
+    }
+  }
+#else
   if (options.keyExists<std::shared_ptr<xacc::NoiseModel>>("noise-model"))
     noise_ = options.get<std::shared_ptr<xacc::NoiseModel>>("noise-model");
+#endif
   buffer = std::move(in_buffer);
   // a noisy simulation always runs shots (:539)
   shots_ = nbShots < 1 ? 1024 : nbShots;
