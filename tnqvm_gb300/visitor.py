@@ -349,7 +349,8 @@ class GpuPmpsVisitor:
         else:
             raise ValueError("Measure more than %d is not supported." % MAX_QUBITS_FOR_DENSITY_MATRIX)
         dm = p.density_matrix(sel)
-        buf.addExtraInfo("density_matrix", [(float(z.real), float(z.imag)) for z in dm.reshape(-1)])
+        # (re, im) rows, one per entry, row-major (a 13-qubit register has 4^13)
+        buf.addExtraInfo("density_matrix", np.stack([dm.real.reshape(-1), dm.imag.reshape(-1)], axis=1))
         seed = int(self.options.get("seed", np.random.SeedSequence().entropy % (1 << 63)))
         bits = p.sample(self.shots, seed)
         if self.noise is not None:
